@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark: FDAS searches/s at 2^21 bins x 85 templates x 8 harmonics on GB300.
+
+One step = one full search of one spectrum: overlap-save tiling + forward FFT,
+FT convolution of all 85 templates into the filter-output plane (FOP), 8-plane
+harmonic summing with chi-square thresholds (FAR 1e-6), FP64 recheck and the
+sorted candidate list.
+
+* ``value``: searches/s with the spectrum already resident in HBM
+  (fdas_enqueue_search_device), timed with CUDA events on the library's stream.
+* ``e2e``: the same metric through the reference-facing call (fdas_launch /
+  fdas_wait) with pinned HOST buffers: the 2^21-bin spectrum is copied in and
+  the 4096-entry candidate list copied out inside every step.
+* ``roofline``: the dominant kernel's algorithmic bytes / its average duration
+  (CUDA events around each stage) against the measured HBM copy bandwidth.
+* ``cpu_baseline``: the oracle port (NumPy/SciPy restatement of the reference's
+  ft_conv.py + hsum.py) on a bounded sample, extrapolated to one search.
+
+``--impl reference`` times the reference's own CPU path (the oracle port of
+ft_conv.py / hsum.py: float32/complex64 like the reference) with all host cores.
+Multi-GPU (torchrun, N > 1): independent replicas, one search stream per rank,
+no collective on the data path; value = all ranks' searches / max time.
+"""
+import argparse
+import json
+import os
+import pathlib
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_BINS = 1 << 21
+N_TEMPLATES = 85
+N_PLANES = 8
+METRIC = "searches/s at 2^21 bins x 85 tmpl x 8 harm"
+UNIT = "searches/s"
+WORKLOAD = {"workload": "FDAS full single-trial search: 2^22-sample Gaussian series -> 2^21 complex64 bins, "
+                        "3 injected accelerated signals (z -30/0/+35), 85 x 421-tap Fresnel template bank, "
+                        "2048-point overlap-save tiles (overlap 420, 1289 tiles), 8 harmonic planes, "
+                        "chi-square thresholds FAR 1e-6, all accelerations",
+            "n_bins": N_BINS, "n_templates": N_TEMPLATES, "n_planes": N_PLANES, "tile": 2048, "overlap": 420,
+            "l2": "inputs larger than L2: each search writes and reads a 713 MB FOP (L2 is 129 MB)"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_fop_rows(args):
+    """FOP rows by direct convolution (ft_conv.py:199-205 semantics)."""
+    from oracle import fdas_oracle as O
+    x, bank, rows, dtype = args
+    return O.fop(x, bank, dtype=dtype, rows=rows)
+
+
+def cpu_search_time(x, bank, thr, n_rows_sample, bin_frac, dtype, workers=1):
+    """Extrapolated time of one CPU search from a bounded sample.
+
+    FOP: ``n_rows_sample`` of the 85 rows by direct linear convolution (scaled
+    by 85 / n_rows_sample).  Harmonic summing: the vectorised restatement of
+    hsum.py over the first ``bin_frac`` of the bins for all rows (scaled by
+    1 / bin_frac).  Returns (seconds per search, description).
+    """
+    from oracle import fdas_oracle as O
+    rows = np.linspace(0, N_TEMPLATES - 1, n_rows_sample).astype(int)
+    t0 = time.perf_counter()
+    if workers > 1:
+        import multiprocessing as mp
+        chunks = np.array_split(rows, workers)
+        with mp.get_context("spawn").Pool(workers) as pool:
+            pool.map(cpu_fop_rows, [(x, bank, list(c), dtype) for c in chunks if len(c)])
+    else:
+        O.fop(x, bank, dtype=dtype, rows=rows)
+    t_fop = (time.perf_counter() - t0) * N_TEMPLATES / n_rows_sample
+    nb = int(x.size * bin_frac)
+    rng = np.random.default_rng(0)
+    plane = rng.exponential(size=(N_TEMPLATES, nb)).astype(dtype)
+    t0 = time.perf_counter()
+    O.detections_streaming(plane, thr, N_PLANES, dtype=dtype)
+    t_hs = (time.perf_counter() - t0) / bin_frac
+    desc = (f"FOP of {n_rows_sample}/85 rows at 2^21 bins (x{N_TEMPLATES / n_rows_sample:.1f}) + vectorised "
+            f"harmonic summing over {nb} of 2^21 bins, 85 rows, 8 planes (x{1 / bin_frac:.0f}); "
+            f"{np.dtype(dtype).name}")
+    return t_fop + t_hs, desc
+
+
+def make_inputs():
+    from fdas_gb300 import synth
+    from fdas_gb300.templates import template_bank
+    samples, _ = synth.full_case()
+    x, _ = synth.spectrum(samples)
+    bank = template_bank()
+    from scipy.stats import gamma
+    thr = np.array([gamma.isf(1e-6, k) for k in range(1, N_PLANES + 1)], dtype=np.float32)
+    return x, bank, thr
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    x, bank, thr = make_inputs()
+    workers = os.cpu_count() or 1
+    times = []
+    desc = ""
+    for i in range(args.warmup + args.steps):
+        t, desc = cpu_search_time(x, bank, thr, n_rows_sample=min(N_TEMPLATES, 2 * workers), bin_frac=1 / 16,
+                                  dtype=np.float32, workers=workers)
+        if i >= args.warmup:
+            times.append(t)
+    v = 1.0 / float(np.mean(times))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": WORKLOAD,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+                             "sample": "per step: " + desc + " (the reference's ft_conv.py + hsum.py path, "
+                                       "restated in NumPy/SciPy at its own float32/complex64 precision)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from fdas_gb300.fdas import FDAS, PinnedArray
+
+    x, bank, thr = make_inputs()
+    log = open(os.devnull, "w")
+    p = FDAS(log)
+    assert p.initialise_accelerator(N_BINS, device=local), p.last_error
+    assert p.upload_templates(bank, FDAS.A), p.last_error
+    assert p.upload_templates(bank, FDAS.B), p.last_error
+    d_x = torch.from_numpy(x.view(np.float32)).to(f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(p.stream(FDAS.A), device=f"cuda:{local}")
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- value: device-resident spectrum, CUDA events on the library stream
+    for _ in range(args.warmup):
+        assert p.enqueue_search_device(d_x.data_ptr(), thr, FDAS.AllAccelerations, FDAS.A), p.last_error
+    assert p.synchronize(FDAS.A)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    stage = np.zeros((args.steps, 6), dtype=np.float64)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        with torch.cuda.stream(stream):
+            evs[0].record(stream)
+            for i in range(args.steps):
+                assert p.enqueue_search_device(d_x.data_ptr(), thr, FDAS.AllAccelerations, FDAS.A), p.last_error
+                evs[i + 1].record(stream)
+                if args.stage_times:
+                    stage[i] = p.stage_times(FDAS.A)
+        assert p.synchronize(FDAS.A)
+        torch.cuda.synchronize()
+    barrier()
+    total_ms = evs[0].elapsed_time(evs[-1])
+    per = np.array([evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)])
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * args.steps / (total_ms / 1e3)
+    rec, n_cand, dropped = p.retrieve_candidate_list(FDAS.A)
+
+    # ---- stage times (separate pass, so the per-launch host syncs do not
+    # disturb the throughput number above)
+    n_stage = min(args.steps, 50)
+    st = []
+    for i in range(n_stage):
+        assert p.enqueue_search_device(d_x.data_ptr(), thr, FDAS.AllAccelerations, FDAS.A)
+        st.append(p.stage_times(FDAS.A))
+    st = np.array(st)
+    names = ["input", "tiling", "ft_convolution", "harmonic_summing", "download", "total"]
+    stage_ms = {n: float(np.mean(st[:, i])) for i, n in enumerate(names)}
+    alg = {"tiling": 8 * N_BINS, "ft_convolution": 4 * N_TEMPLATES * N_BINS,
+           "harmonic_summing": 4 * N_TEMPLATES * N_BINS}
+    dom = max(alg, key=lambda k: stage_ms[k])
+    peak, peak_kind = measured_peaks()
+    achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(dom)
+
+    # ---- e2e: pinned host buffers through fdas_launch / fdas_wait, A/B sets
+    hx = {ab: PinnedArray((N_BINS,), np.complex64) for ab in (FDAS.A, FDAS.B)}
+    for ab in hx:
+        hx[ab].array[:] = x
+    n_list = p.get_candidate_list_sz()
+    hl = {ab: PinnedArray((n_list,), np.uint32) for ab in (FDAS.A, FDAS.B)}
+    hp = {ab: PinnedArray((n_list,), np.float32) for ab in (FDAS.A, FDAS.B)}
+    e2e_steps = args.steps
+    for i in range(args.warmup):
+        ab = i & 1
+        assert p.launch(hx[ab].array, thr, hl[ab].array, hp[ab].array, FDAS.AllAccelerations, ab)
+        assert p.wait(ab)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        ab = i & 1
+        assert p.launch(hx[ab].array, thr, hl[ab].array, hp[ab].array, FDAS.AllAccelerations, ab), p.last_error
+        if i > 0:
+            assert p.wait(1 - ab), p.last_error
+    assert p.wait((e2e_steps - 1) & 1)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = ws * e2e_steps / e2e_s
+
+    if rank != 0:
+        return
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        t_cpu, desc = cpu_search_time(x, bank, thr, n_rows_sample=4, bin_frac=1 / 32, dtype=np.float32)
+        cpu = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "one search extrapolated from: " + desc}
+    launches_per_search = 5  # tiling, FT convolution, harmonic summing, FP64 recheck, sort/finalize
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "config": dict(WORKLOAD, parallelism=f"replicas{ws}"),
+        "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
+        "stage_ms": stage_ms, "candidates": int(n_cand), "candidates_dropped": int(dropped),
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg[dom], "traffic": traffic},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * N_BINS,
+                "d2h_bytes_per_step": 8 * n_list},
+        "gpu_launches": launches_per_search * args.steps,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--stage-times", action="store_true", help="per-step stage events inside the timed loop")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

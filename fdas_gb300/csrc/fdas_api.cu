@@ -1,0 +1,892 @@
+// Host orchestration behind the C ABI (include/fdas_gb300.h).
+//
+// Mirrors the reference's host class FDAS (fdas/src/host/FDAS.cpp): two buffer
+// sets A/B, each with its own CUDA stream in place of the OpenCL command
+// queues, CUDA events in place of cl::Event for the stage timings, and the
+// same enqueue order: input copy -> tiling -> FT convolution -> harmonic
+// summing -> candidate download.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fdas_gb300.h"
+#include "kernels.cuh"
+
+using namespace fdas;
+
+namespace {
+
+thread_local std::string g_init_error;
+
+constexpr int kCtrlStatus = 0;
+constexpr int kCtrlRecheckCount = 1;
+constexpr int kCtrlCount = 2;  // + plane
+constexpr int kCtrlWords = 2 + kMaxPlanes;
+constexpr int kRecheckCap = 65536;
+constexpr int kNumEvents = 6;  // start, input, tiling, ftc, hsum, done
+
+struct BufferSet {
+  cudaStream_t stream = nullptr;
+  float2 *d_input = nullptr;
+  const float2 *cur_input = nullptr;
+  float2 *d_tiles = nullptr;
+  float2 *d_tmpl = nullptr;
+  double2 *d_taps = nullptr;
+  int *d_taplen = nullptr;
+  float *d_fop = nullptr;
+  unsigned long long *d_key = nullptr;
+  float *d_pwr = nullptr;
+  unsigned *d_ctrl = nullptr;
+  unsigned *h_ctrl = nullptr;  // pinned mirror of d_ctrl
+  uint4 *d_rc = nullptr;
+  uint32_t *d_cloc = nullptr;
+  float *d_cpwr = nullptr;
+  cudaEvent_t ev[kNumEvents] = {};
+  bool have_templates = false;
+  bool have_taps = false;
+  bool have_input = false;
+  bool fop_from_input = false;
+  bool launched = false;
+  bool ctrl_valid = false;
+  std::vector<float> thresholds;
+  // harmonic summing held back by sync_pipeline
+  bool pending = false;
+  std::vector<float> p_thr;
+  fdas_fop_part p_which = FDAS_ALL_ACCELERATIONS;
+  uint32_t *p_loc = nullptr;
+  float *p_pwr = nullptr;
+  bool ev_ftc_recorded = false;
+};
+
+}  // namespace
+
+struct fdas_handle {
+  fdas_config cfg{};
+  int N = 0, T = 0, H = 0, L = 0, O = 0, payload = 0, n_tiles = 0, P = 0, cap = 0, per_plane = 0;
+  long long stride = 0;
+  int tap_pitch = 0;
+  std::string err;
+  fdas_log_fn log_fn = nullptr;
+  void *log_user = nullptr;
+  float2 *d_twiddle = nullptr;
+  double2 *d_twiddle64 = nullptr;
+  BufferSet set[2];
+  // print_stats bookkeeping
+  float pipeline_accum_ms = 0.f;
+  unsigned pipeline_launches = 0;
+  cudaEvent_t pipeline_start = nullptr;
+};
+
+namespace {
+
+void logf(fdas_handle *h, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h && h->log_fn) h->log_fn(buf, h->log_user);
+  else fprintf(stderr, "%s\n", buf);
+}
+
+fdas_status fail(fdas_handle *h, fdas_status st, const std::string &msg) {
+  if (h) h->err = msg;
+  else g_init_error = msg;
+  return st;
+}
+
+fdas_status cuda_fail(fdas_handle *h, cudaError_t e, const char *what, const char *file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "CUDA call failed with %s (%s): %s [%s:%d]", cudaGetErrorName(e),
+           cudaGetErrorString(e), what, file, line);
+  if (h) logf(h, "[ERROR] %s", buf);
+  return fail(h, e == cudaErrorMemoryAllocation ? FDAS_ERR_OUT_OF_MEMORY : FDAS_ERR_CUDA, buf);
+}
+
+#define CK(h, expr)                                                  \
+  do {                                                               \
+    cudaError_t e_ = (expr);                                         \
+    if (e_ != cudaSuccess) return cuda_fail((h), e_, #expr, __FILE__, __LINE__); \
+  } while (0)
+
+bool valid_set(fdas_buffer_set ab) { return ab == FDAS_SET_A || ab == FDAS_SET_B; }
+bool valid_part(fdas_fop_part w) {
+  return w == FDAS_NEGATIVE_ACCELERATIONS || w == FDAS_POSITIVE_ACCELERATIONS || w == FDAS_ALL_ACCELERATIONS;
+}
+
+#define CHECK_HANDLE(h)                                                              \
+  do {                                                                               \
+    if (!(h)) return fail(nullptr, FDAS_ERR_INVALID_ARG, "null handle");             \
+  } while (0)
+#define CHECK_SET(h, ab)                                                             \
+  do {                                                                               \
+    if (!valid_set(ab)) return fail((h), FDAS_ERR_INVALID_ARG, "invalid buffer set"); \
+  } while (0)
+
+int bitrev2(int x) { return ((x & 1) << 1) | ((x >> 1) & 1); }
+
+// p4 position 4 s + j holds natural bin bitrev2(j) * 512 + s (tmpl-gen.py:145-153)
+void p4_to_natural(const fdas_complex *p4, fdas_complex *nat) {
+  for (int s = 0; s < 512; ++s)
+    for (int j = 0; j < 4; ++j) nat[bitrev2(j) * 512 + s] = p4[4 * s + j];
+}
+void natural_to_p4(const float2 *nat, fdas_complex *p4) {
+  for (int s = 0; s < 512; ++s)
+    for (int j = 0; j < 4; ++j) {
+      const float2 v = nat[bitrev2(j) * 512 + s];
+      p4[4 * s + j] = fdas_complex{v.x, v.y};
+    }
+}
+
+void rows_of(const fdas_handle *h, fdas_fop_part w, int *row_begin, int *n_rows) {
+  if (w == FDAS_NEGATIVE_ACCELERATIONS) { *row_begin = 0; *n_rows = h->H + 1; }
+  else if (w == FDAS_POSITIVE_ACCELERATIONS) { *row_begin = h->H; *n_rows = h->H + 1; }
+  else { *row_begin = 0; *n_rows = h->T; }
+}
+
+// ---------------------------------------------------------------- stages
+fdas_status enqueue_input(fdas_handle *h, int ab, const fdas_complex *input, bool device_ptr) {
+  BufferSet &S = h->set[ab];
+  if (!input) return fail(h, FDAS_ERR_INVALID_ARG, "input is NULL");
+  CK(h, cudaEventRecord(S.ev[0], S.stream));
+  if (h->cfg.sync_pipeline && h->set[1 - ab].ev_ftc_recorded)
+    CK(h, cudaStreamWaitEvent(S.stream, h->set[1 - ab].ev[3], 0));  // FDAS.cpp:287-288
+  if (device_ptr) {
+    S.cur_input = reinterpret_cast<const float2 *>(input);
+  } else {
+    CK(h, cudaMemcpyAsync(S.d_input, input, sizeof(float2) * (size_t)h->N, cudaMemcpyHostToDevice, S.stream));
+    S.cur_input = S.d_input;
+  }
+  CK(h, cudaEventRecord(S.ev[1], S.stream));
+  S.have_input = true;
+  return FDAS_OK;
+}
+
+fdas_status enqueue_tiling(fdas_handle *h, int ab) {
+  BufferSet &S = h->set[ab];
+  TileParams p{};
+  p.input = S.cur_input;
+  p.n_bins = h->N;
+  p.n_tiles = h->n_tiles;
+  p.overlap = h->O;
+  p.payload = h->payload;
+  p.tiles = S.d_tiles;
+  p.twiddle = h->d_twiddle;
+  CK(h, launch_tile_fft(p, S.stream));
+  CK(h, cudaEventRecord(S.ev[2], S.stream));
+  return FDAS_OK;
+}
+
+fdas_status enqueue_ftc(fdas_handle *h, int ab, fdas_fop_part which) {
+  BufferSet &S = h->set[ab];
+  if (!S.have_templates) return fail(h, FDAS_ERR_STATE, "templates not uploaded for this buffer set");
+  if (!S.have_input) return fail(h, FDAS_ERR_STATE, "no input tiled on this buffer set");
+  FtcParams p{};
+  p.tiles = S.d_tiles;
+  p.tmpl = S.d_tmpl;
+  p.fop = S.d_fop;
+  p.fop_stride = h->stride;
+  p.n_bins = h->N;
+  p.n_tiles = h->n_tiles;
+  p.overlap = h->O;
+  p.payload = h->payload;
+  rows_of(h, which, &p.row_begin, &p.n_rows);
+  p.twiddle = h->d_twiddle;
+  CK(h, launch_ftc(p, S.stream));
+  CK(h, cudaEventRecord(S.ev[3], S.stream));
+  S.ev_ftc_recorded = true;
+  S.fop_from_input = true;
+  return FDAS_OK;
+}
+
+fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_part which) {
+  BufferSet &S = h->set[ab];
+  const float *thr = thr_in;
+  if (!thr) {
+    if (S.thresholds.empty()) return fail(h, FDAS_ERR_STATE, "no thresholds given or uploaded");
+    thr = S.thresholds.data();
+  }
+  const int P = h->P;
+  const bool recheck = h->cfg.recheck && S.fop_from_input && S.have_taps && S.cur_input;
+  const float band_rel = h->cfg.recheck_band > 0.f ? h->cfg.recheck_band : 1e-4f;
+
+  HsumParams p{};
+  p.fop = S.d_fop;
+  p.stride = h->stride;
+  p.n_bins = h->N;
+  p.half = h->H;
+  p.n_planes = P;
+  const int H = h->H;
+  if (which == FDAS_NEGATIVE_ACCELERATIONS) { p.tlo[0] = 0; p.tlo[1] = H + 1; }
+  else if (which == FDAS_POSITIVE_ACCELERATIONS) { p.tlo[0] = H + 1; p.tlo[1] = 0; }
+  else { p.tlo[0] = 1; p.tlo[1] = 0; }
+  for (int j = 0; j < kMaxPlanes; ++j) {
+    const float t = j < P ? thr[j] : INFINITY;
+    if (recheck) {
+      const float band = band_rel * std::fabs(t);
+      p.hi[j] = t + band;
+      p.lo[j] = t - band;
+      p.trig[j] = p.lo[j];
+    } else {
+      p.hi[j] = t;
+      p.lo[j] = INFINITY;
+      p.trig[j] = t;
+    }
+  }
+  int off = 0;
+  unsigned bytes = 0;
+  for (int j = 2; j <= P; ++j) {
+    p.srows[j] = H / j + 1;
+    p.sw[j] = ((kHsBins - 1) / j + 5 + 3) & ~3;
+    p.soff[j] = off;
+    off += p.srows[j] * p.sw[j];
+    bytes += (unsigned)(p.srows[j] * p.sw[j] * 4);
+  }
+  p.smem_floats = off;
+  p.stage_bytes = bytes;
+  p.cand_key = S.d_key;
+  p.cand_pwr = S.d_pwr;
+  p.cand_count = S.d_ctrl + kCtrlCount;
+  p.cand_cap = h->cap;
+  p.rc_list = S.d_rc;
+  p.rc_count = S.d_ctrl + kCtrlRecheckCount;
+  p.rc_cap = kRecheckCap;
+  p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlStatus);
+  p.timeout_ns = 2000000000LL;  // 2 s
+
+  CK(h, cudaMemsetAsync(S.d_ctrl, 0, sizeof(unsigned) * kCtrlWords, S.stream));
+  CK(h, launch_hsum(p, S.stream));
+  if (recheck) {
+    RecheckParams r{};
+    r.input = S.cur_input;
+    r.n_bins = h->N;
+    r.half = H;
+    r.taps = S.d_taps;
+    r.tap_len = S.d_taplen;
+    r.tap_pitch = h->tap_pitch;
+    for (int j = 0; j < kMaxPlanes; ++j) r.thr[j] = j < P ? (double)thr[j] : INFINITY;
+    r.rc_list = S.d_rc;
+    r.rc_count = S.d_ctrl + kCtrlRecheckCount;
+    r.rc_cap = kRecheckCap;
+    r.cand_key = S.d_key;
+    r.cand_pwr = S.d_pwr;
+    r.cand_count = S.d_ctrl + kCtrlCount;
+    r.cand_cap = h->cap;
+    r.status = p.status;
+    CK(h, launch_recheck(r, S.stream));
+  }
+  FinalizeParams f{};
+  f.cand_key = S.d_key;
+  f.cand_pwr = S.d_pwr;
+  f.cand_count = S.d_ctrl + kCtrlCount;
+  f.cand_cap = h->cap;
+  f.per_plane = h->per_plane;
+  f.compat_loc = S.d_cloc;
+  f.compat_pwr = S.d_cpwr;
+  f.invalid_location = (0u << 29) | ((uint32_t)((h->H + 1 + h->H) & 0x7f) << 22);  // encode(1, H+1, 0)
+  CK(h, launch_finalize(f, P, S.stream));
+  CK(h, cudaMemcpyAsync(S.h_ctrl, S.d_ctrl, sizeof(unsigned) * kCtrlWords, cudaMemcpyDeviceToHost, S.stream));
+  CK(h, cudaEventRecord(S.ev[4], S.stream));
+  S.ctrl_valid = true;
+  return FDAS_OK;
+}
+
+fdas_status enqueue_download(fdas_handle *h, int ab, uint32_t *loc, float *pwr) {
+  BufferSet &S = h->set[ab];
+  const size_t n = (size_t)h->P * h->per_plane;
+  if (loc) CK(h, cudaMemcpyAsync(loc, S.d_cloc, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, S.stream));
+  if (pwr) CK(h, cudaMemcpyAsync(pwr, S.d_cpwr, sizeof(float) * n, cudaMemcpyDeviceToHost, S.stream));
+  CK(h, cudaEventRecord(S.ev[5], S.stream));
+  S.launched = true;
+  return FDAS_OK;
+}
+
+fdas_status release_pending(fdas_handle *h, int ab) {
+  BufferSet &S = h->set[ab];
+  if (!S.pending) return FDAS_OK;
+  S.pending = false;
+  fdas_status st = enqueue_hsum(h, ab, S.p_thr.data(), S.p_which);
+  if (st != FDAS_OK) return st;
+  return enqueue_download(h, ab, S.p_loc, S.p_pwr);
+}
+
+fdas_status sync_set(fdas_handle *h, int ab) {
+  BufferSet &S = h->set[ab];
+  CK(h, cudaStreamSynchronize(S.stream));
+  if (S.ctrl_valid && (S.h_ctrl[kCtrlStatus] & kStatusHsumTimeout))
+    return fail(h, FDAS_ERR_TIMEOUT, "harmonic summing: shared-memory staging timed out");
+  return FDAS_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return -1.f;
+  }
+  return ms;
+}
+
+void free_set(BufferSet &S) {
+  if (S.stream) cudaStreamSynchronize(S.stream);
+  cudaFree(S.d_input);
+  cudaFree(S.d_tiles);
+  cudaFree(S.d_tmpl);
+  cudaFree(S.d_taps);
+  cudaFree(S.d_taplen);
+  cudaFree(S.d_fop);
+  cudaFree(S.d_key);
+  cudaFree(S.d_pwr);
+  cudaFree(S.d_ctrl);
+  cudaFree(S.d_rc);
+  cudaFree(S.d_cloc);
+  cudaFree(S.d_cpwr);
+  if (S.h_ctrl) cudaFreeHost(S.h_ctrl);
+  for (auto &e : S.ev)
+    if (e) cudaEventDestroy(e);
+  if (S.stream) cudaStreamDestroy(S.stream);
+  S = BufferSet();
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+const char *fdas_version(void) { return "fdas_gb300 0.1 (sm_103a)"; }
+
+void fdas_default_config(fdas_config *cfg, uint32_t n_frequency_bins) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->n_frequency_bins = n_frequency_bins;
+  cfg->n_templates = 85;
+  cfg->max_template_len = 421;
+  cfg->tile_overlap = 0;
+  cfg->n_planes = 8;
+  cfg->candidate_capacity = 0;
+  cfg->candidates_per_plane_compat = 0;
+  cfg->device = 0;
+  cfg->buffer_mode = FDAS_MODE_PER_SET;
+  cfg->sync_pipeline = 0;
+  cfg->recheck = 1;
+  cfg->recheck_band = 0.f;
+}
+
+const char *fdas_last_error(const fdas_handle *h) { return h ? h->err.c_str() : g_init_error.c_str(); }
+
+fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle **out) {
+  if (!out) return fail(nullptr, FDAS_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if (!cfg_in) return fail(nullptr, FDAS_ERR_INVALID_ARG, "config is NULL");
+  fdas_config cfg = *cfg_in;
+  if (cfg.n_frequency_bins == 0) return fail(nullptr, FDAS_ERR_INVALID_ARG, "n_frequency_bins must be > 0");
+  if (cfg.n_frequency_bins > (1u << 30)) return fail(nullptr, FDAS_ERR_INVALID_ARG, "n_frequency_bins too large");
+  if (cfg.n_templates == 0 || cfg.n_templates % 2 == 0 || cfg.n_templates > 127)
+    return fail(nullptr, FDAS_ERR_INVALID_ARG, "n_templates must be odd and at most 127");
+  if (cfg.n_planes < 1 || cfg.n_planes > (uint32_t)kMaxPlanes)
+    return fail(nullptr, FDAS_ERR_INVALID_ARG, "n_planes must be in 1..16");
+  if (cfg.max_template_len < 1) return fail(nullptr, FDAS_ERR_INVALID_ARG, "max_template_len must be >= 1");
+  uint32_t O = cfg.tile_overlap ? cfg.tile_overlap : ((cfg.max_template_len - 1 + 3) / 4) * 4;
+  if (O + 1 < cfg.max_template_len)
+    return fail(nullptr, FDAS_ERR_INVALID_ARG, "tile_overlap must be >= max_template_len - 1 (overlap-save)");
+  if (O >= (uint32_t)kTile) return fail(nullptr, FDAS_ERR_INVALID_ARG, "tile_overlap must be < 2048");
+  uint32_t cap = cfg.candidate_capacity ? cfg.candidate_capacity : (uint32_t)kSortCap;
+  if (cap > (uint32_t)kSortCap) return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidate_capacity must be <= 8192");
+  uint32_t pc = cfg.candidates_per_plane_compat ? cfg.candidates_per_plane_compat : 512u;
+  if (pc > cap) return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidates_per_plane_compat must be <= capacity");
+
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(nullptr, FDAS_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (cfg.device < 0 || cfg.device >= ndev) return fail(nullptr, FDAS_ERR_INVALID_ARG, "invalid device ordinal");
+  e = cudaSetDevice(cfg.device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice", __FILE__, __LINE__);
+
+  fdas_handle *h = new fdas_handle();
+  h->cfg = cfg;
+  h->cfg.tile_overlap = O;
+  h->cfg.candidate_capacity = cap;
+  h->cfg.candidates_per_plane_compat = pc;
+  h->N = (int)cfg.n_frequency_bins;
+  h->T = (int)cfg.n_templates;
+  h->H = h->T / 2;
+  h->L = (int)cfg.max_template_len;
+  h->O = (int)O;
+  h->payload = kTile - h->O;
+  h->n_tiles = (h->N + h->payload - 1) / h->payload;  // FDAS.cpp:177-183
+  h->P = (int)cfg.n_planes;
+  h->cap = (int)cap;
+  h->per_plane = (int)pc;
+  h->stride = ((long long)h->N + kHsBins - 1) / kHsBins * kHsBins;
+  h->tap_pitch = std::max(h->L, h->O + 1);
+
+  auto bail = [&](fdas_status st) {
+    g_init_error = h->err;
+    for (auto &S : h->set) free_set(S);
+    cudaFree(h->d_twiddle);
+    cudaFree(h->d_twiddle64);
+    delete h;
+    return st;
+  };
+
+  // twiddle tables, computed on the host in double precision
+  {
+    std::vector<float2> tw(kTile);
+    std::vector<double2> tw64(kTile);
+    for (int j = 0; j < kTile; ++j) {
+      const double a = 2.0 * M_PI * (double)j / (double)kTile;
+      tw[j] = make_float2((float)std::cos(a), (float)std::sin(a));
+      tw64[j] = make_double2(std::cos(a), -std::sin(a));
+    }
+    if ((e = cudaMalloc(&h->d_twiddle, sizeof(float2) * kTile)) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_twiddle64, sizeof(double2) * kTile)) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_twiddle, tw.data(), sizeof(float2) * kTile, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_twiddle64, tw64.data(), sizeof(double2) * kTile, cudaMemcpyHostToDevice)) !=
+            cudaSuccess) {
+      cuda_fail(h, e, "twiddle tables", __FILE__, __LINE__);
+      return bail(e == cudaErrorMemoryAllocation ? FDAS_ERR_OUT_OF_MEMORY : FDAS_ERR_CUDA);
+    }
+  }
+
+  const size_t fop_floats = (size_t)h->T * (size_t)h->stride + 4096;
+  for (int ab = 0; ab < 2; ++ab) {
+    BufferSet &S = h->set[ab];
+    struct A {
+      void **p;
+      size_t bytes;
+    } allocs[] = {
+        {(void **)&S.d_input, sizeof(float2) * ((size_t)h->N + 64)},
+        {(void **)&S.d_tiles, sizeof(float2) * (size_t)h->n_tiles * kTile},
+        {(void **)&S.d_tmpl, sizeof(float2) * (size_t)h->T * kTile},
+        {(void **)&S.d_taps, sizeof(double2) * (size_t)h->T * h->tap_pitch},
+        {(void **)&S.d_taplen, sizeof(int) * (size_t)h->T},
+        {(void **)&S.d_fop, sizeof(float) * fop_floats},
+        {(void **)&S.d_key, sizeof(unsigned long long) * (size_t)h->P * h->cap},
+        {(void **)&S.d_pwr, sizeof(float) * (size_t)h->P * h->cap},
+        {(void **)&S.d_ctrl, sizeof(unsigned) * kCtrlWords},
+        {(void **)&S.d_rc, sizeof(uint4) * kRecheckCap},
+        {(void **)&S.d_cloc, sizeof(uint32_t) * (size_t)h->P * h->per_plane},
+        {(void **)&S.d_cpwr, sizeof(float) * (size_t)h->P * h->per_plane},
+    };
+    for (auto &a : allocs) {
+      if ((e = cudaMalloc(a.p, a.bytes)) != cudaSuccess) {
+        char msg[160];
+        snprintf(msg, sizeof(msg), "device allocation of %zu bytes", a.bytes);
+        cuda_fail(h, e, msg, __FILE__, __LINE__);
+        return bail(FDAS_ERR_OUT_OF_MEMORY);
+      }
+    }
+    if ((e = cudaMemset(S.d_fop, 0, sizeof(float) * fop_floats)) != cudaSuccess ||
+        (e = cudaMemset(S.d_ctrl, 0, sizeof(unsigned) * kCtrlWords)) != cudaSuccess ||
+        (e = cudaHostAlloc((void **)&S.h_ctrl, sizeof(unsigned) * kCtrlWords, cudaHostAllocDefault)) !=
+            cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking)) != cudaSuccess) {
+      cuda_fail(h, e, "buffer set initialisation", __FILE__, __LINE__);
+      return bail(FDAS_ERR_CUDA);
+    }
+    std::memset(S.h_ctrl, 0, sizeof(unsigned) * kCtrlWords);
+    for (auto &ev : S.ev) {
+      if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
+        cuda_fail(h, e, "cudaEventCreate", __FILE__, __LINE__);
+        return bail(FDAS_ERR_CUDA);
+      }
+    }
+  }
+  logf(h, "[INFO] Device %d: %d bins, %d templates, %d tiles (overlap %d), %d planes", cfg.device, h->N, h->T,
+       h->n_tiles, h->O, h->P);
+  *out = h;
+  return FDAS_OK;
+}
+
+void fdas_destroy(fdas_handle *h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  for (auto &S : h->set) free_set(S);
+  cudaFree(h->d_twiddle);
+  cudaFree(h->d_twiddle64);
+  if (h->pipeline_start) cudaEventDestroy(h->pipeline_start);
+  delete h;
+}
+
+fdas_status fdas_upload_templates(fdas_handle *h, const fdas_complex *templates, fdas_template_layout layout,
+                                  fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!templates) return fail(h, FDAS_ERR_INVALID_ARG, "templates is NULL");
+  CK(h, cudaSetDevice(h->cfg.device));
+  BufferSet &S = h->set[ab];
+  const int T = h->T;
+  if (layout == FDAS_TEMPLATES_TIME_DOMAIN) {
+    // ft_conv.py:203 convolves with the non-zero taps of each row
+    std::vector<double2> taps((size_t)T * h->tap_pitch, make_double2(0.0, 0.0));
+    std::vector<int> len(T, 0);
+    for (int r = 0; r < T; ++r) {
+      int n = 0;
+      for (int q = 0; q < h->L; ++q) {
+        const fdas_complex c = templates[(size_t)r * h->L + q];
+        if (c.re != 0.f || c.im != 0.f) taps[(size_t)r * h->tap_pitch + n++] = make_double2(c.re, c.im);
+      }
+      if (n > h->O + 1)
+        return fail(h, FDAS_ERR_INVALID_ARG, "template has more non-zero taps than tile_overlap + 1");
+      len[r] = n;
+    }
+    CK(h, cudaMemcpy(S.d_taps, taps.data(), sizeof(double2) * taps.size(), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(S.d_taplen, len.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+    SpectraParams p{};
+    p.taps = S.d_taps;
+    p.tap_len = S.d_taplen;
+    p.tap_pitch = h->tap_pitch;
+    p.n_templates = T;
+    p.twiddle64 = h->d_twiddle64;
+    p.spectra = S.d_tmpl;
+    CK(h, launch_spectra(p, S.stream));
+    CK(h, cudaStreamSynchronize(S.stream));
+  } else if (layout == FDAS_TEMPLATES_FFT_P4 || layout == FDAS_TEMPLATES_FFT_NATURAL) {
+    std::vector<fdas_complex> nat((size_t)T * kTile);
+    for (int r = 0; r < T; ++r) {
+      if (layout == FDAS_TEMPLATES_FFT_P4) p4_to_natural(templates + (size_t)r * kTile, nat.data() + (size_t)r * kTile);
+      else std::memcpy(nat.data() + (size_t)r * kTile, templates + (size_t)r * kTile, sizeof(fdas_complex) * kTile);
+    }
+    // unscaled spectra -> FP64 taps for the recheck (via the tiles buffer as scratch
+    // would clash with a tiled input; use the template buffer before scaling)
+    CK(h, cudaMemcpy(S.d_tmpl, nat.data(), sizeof(float2) * nat.size(), cudaMemcpyHostToDevice));
+    TapsParams tp{};
+    tp.spectra = S.d_tmpl;
+    tp.n_templates = T;
+    tp.n_taps = h->O + 1;
+    tp.twiddle64 = h->d_twiddle64;
+    tp.taps = S.d_taps;
+    tp.tap_len = S.d_taplen;
+    tp.tap_pitch = h->tap_pitch;
+    CK(h, launch_taps(tp, S.stream));
+    CK(h, cudaStreamSynchronize(S.stream));
+    // 1/2048 of the inverse transform folded into the template spectra (exact)
+    for (auto &c : nat) {
+      c.re *= 1.0f / 2048.0f;
+      c.im *= 1.0f / 2048.0f;
+    }
+    CK(h, cudaMemcpy(S.d_tmpl, nat.data(), sizeof(float2) * nat.size(), cudaMemcpyHostToDevice));
+  } else {
+    return fail(h, FDAS_ERR_INVALID_ARG, "unknown template layout");
+  }
+  S.have_templates = true;
+  S.have_taps = true;
+  logf(h, "[INFO] Uploaded template coefficients");
+  return FDAS_OK;
+}
+
+fdas_status fdas_upload_thresholds(fdas_handle *h, const float *thresholds, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!thresholds) return fail(h, FDAS_ERR_INVALID_ARG, "thresholds is NULL");
+  h->set[ab].thresholds.assign(thresholds, thresholds + h->P);
+  logf(h, "[INFO] Uploaded thresholds");
+  return FDAS_OK;
+}
+
+fdas_status fdas_perform_input_tiling(fdas_handle *h, const fdas_complex *input, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st = enqueue_input(h, ab, input, false);
+  if (st != FDAS_OK) return st;
+  if ((st = enqueue_tiling(h, ab)) != FDAS_OK) return st;
+  if ((st = sync_set(h, ab)) != FDAS_OK) return st;
+  logf(h, "[INFO] Preparation duration: %.3f ms", elapsed(h->set[ab].ev[1], h->set[ab].ev[2]));
+  return FDAS_OK;
+}
+
+fdas_status fdas_perform_ft_convolution(fdas_handle *h, fdas_fop_part which, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!valid_part(which)) return fail(h, FDAS_ERR_INVALID_ARG, "invalid FOP part");
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st = enqueue_ftc(h, ab, which);
+  if (st != FDAS_OK) return st;
+  if ((st = sync_set(h, ab)) != FDAS_OK) return st;
+  logf(h, "[INFO] FT convolution and IFFT duration: %.3f ms", elapsed(h->set[ab].ev[2], h->set[ab].ev[3]));
+  return FDAS_OK;
+}
+
+fdas_status fdas_perform_harmonic_summing(fdas_handle *h, const float *thresholds, fdas_fop_part which,
+                                          fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!valid_part(which)) return fail(h, FDAS_ERR_INVALID_ARG, "invalid FOP part");
+  CK(h, cudaSetDevice(h->cfg.device));
+  BufferSet &S = h->set[ab];
+  CK(h, cudaEventRecord(S.ev[3], S.stream));
+  fdas_status st = enqueue_hsum(h, ab, thresholds, which);
+  if (st != FDAS_OK) return st;
+  if ((st = sync_set(h, ab)) != FDAS_OK) return st;
+  logf(h, "[INFO] Harmonic summing duration: %.3f ms", elapsed(S.ev[3], S.ev[4]));
+  return FDAS_OK;
+}
+
+fdas_status fdas_launch(fdas_handle *h, const fdas_complex *input, const float *thresholds,
+                        uint32_t *detection_location, float *detection_power, fdas_fop_part which,
+                        fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!valid_part(which)) return fail(h, FDAS_ERR_INVALID_ARG, "invalid FOP part");
+  if (!thresholds && h->set[ab].thresholds.empty())
+    return fail(h, FDAS_ERR_STATE, "no thresholds given or uploaded");
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st;
+  // FDAS.cpp:549-550: launching releases the other set's held-back stage
+  if (h->cfg.sync_pipeline && (st = release_pending(h, 1 - ab)) != FDAS_OK) return st;
+  if ((st = enqueue_input(h, ab, input, false)) != FDAS_OK) return st;
+  if ((st = enqueue_tiling(h, ab)) != FDAS_OK) return st;
+  if ((st = enqueue_ftc(h, ab, which)) != FDAS_OK) return st;
+  BufferSet &S = h->set[ab];
+  if (h->cfg.sync_pipeline) {
+    S.pending = true;
+    const float *thr = thresholds ? thresholds : S.thresholds.data();
+    S.p_thr.assign(thr, thr + h->P);
+    S.p_which = which;
+    S.p_loc = detection_location;
+    S.p_pwr = detection_power;
+    S.launched = true;
+    return FDAS_OK;
+  }
+  if ((st = enqueue_hsum(h, ab, thresholds, which)) != FDAS_OK) return st;
+  return enqueue_download(h, ab, detection_location, detection_power);
+}
+
+fdas_status fdas_enqueue_search_device(fdas_handle *h, const fdas_complex *d_input, const float *thresholds,
+                                       fdas_fop_part which, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!valid_part(which)) return fail(h, FDAS_ERR_INVALID_ARG, "invalid FOP part");
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st;
+  if ((st = enqueue_input(h, ab, d_input, true)) != FDAS_OK) return st;
+  if ((st = enqueue_tiling(h, ab)) != FDAS_OK) return st;
+  if ((st = enqueue_ftc(h, ab, which)) != FDAS_OK) return st;
+  if ((st = enqueue_hsum(h, ab, thresholds, which)) != FDAS_OK) return st;
+  return enqueue_download(h, ab, nullptr, nullptr);
+}
+
+fdas_status fdas_synchronize(fdas_handle *h, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  CK(h, cudaSetDevice(h->cfg.device));
+  return sync_set(h, ab);
+}
+
+void *fdas_get_stream(fdas_handle *h, fdas_buffer_set ab) {
+  if (!h || !valid_set(ab)) return nullptr;
+  return (void *)h->set[ab].stream;
+}
+
+fdas_status fdas_wait(fdas_handle *h, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  BufferSet &S = h->set[ab];
+  if (S.pending)
+    return fail(h, FDAS_ERR_STATE,
+                "harmonic summing of this set is held back by sync_pipeline: launch the other set or call "
+                "end_pipeline first");
+  if (!S.launched) return fail(h, FDAS_ERR_STATE, "nothing launched on this buffer set");
+  CK(h, cudaSetDevice(h->cfg.device));
+  CK(h, cudaEventSynchronize(S.ev[5]));
+  if (S.ctrl_valid && (S.h_ctrl[kCtrlStatus] & kStatusHsumTimeout))
+    return fail(h, FDAS_ERR_TIMEOUT, "harmonic summing: shared-memory staging timed out");
+  return FDAS_OK;
+}
+
+fdas_status fdas_end_pipeline(fdas_handle *h, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  CK(h, cudaSetDevice(h->cfg.device));
+  return release_pending(h, 1 - ab);
+}
+
+fdas_status fdas_retrieve_tiles(fdas_handle *h, fdas_complex *tiles, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!tiles) return fail(h, FDAS_ERR_INVALID_ARG, "tiles is NULL");
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st = sync_set(h, ab);
+  if (st != FDAS_OK) return st;
+  std::vector<float2> nat((size_t)h->n_tiles * kTile);
+  CK(h, cudaMemcpy(nat.data(), h->set[ab].d_tiles, sizeof(float2) * nat.size(), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < h->n_tiles; ++i) natural_to_p4(nat.data() + (size_t)i * kTile, tiles + (size_t)i * kTile);
+  return FDAS_OK;
+}
+
+fdas_status fdas_retrieve_fop(fdas_handle *h, float *fop, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!fop) return fail(h, FDAS_ERR_INVALID_ARG, "fop is NULL");
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st = sync_set(h, ab);
+  if (st != FDAS_OK) return st;
+  CK(h, cudaMemcpy2D(fop, sizeof(float) * h->N, h->set[ab].d_fop, sizeof(float) * h->stride, sizeof(float) * h->N,
+                     h->T, cudaMemcpyDeviceToHost));
+  return FDAS_OK;
+}
+
+fdas_status fdas_inject_fop(fdas_handle *h, const float *fop, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!fop) return fail(h, FDAS_ERR_INVALID_ARG, "fop is NULL");
+  CK(h, cudaSetDevice(h->cfg.device));
+  BufferSet &S = h->set[ab];
+  CK(h, cudaStreamSynchronize(S.stream));
+  CK(h, cudaMemcpy2D(S.d_fop, sizeof(float) * h->stride, fop, sizeof(float) * h->N, sizeof(float) * h->N, h->T,
+                     cudaMemcpyHostToDevice));
+  S.fop_from_input = false;
+  return FDAS_OK;
+}
+
+fdas_status fdas_retrieve_candidates(fdas_handle *h, uint32_t *detection_location, float *detection_power,
+                                     fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!detection_location || !detection_power) return fail(h, FDAS_ERR_INVALID_ARG, "output is NULL");
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st = sync_set(h, ab);
+  if (st != FDAS_OK) return st;
+  const size_t n = (size_t)h->P * h->per_plane;
+  CK(h, cudaMemcpy(detection_location, h->set[ab].d_cloc, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+  CK(h, cudaMemcpy(detection_power, h->set[ab].d_cpwr, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  return FDAS_OK;
+}
+
+fdas_status fdas_retrieve_candidate_list(fdas_handle *h, fdas_candidate *out, uint32_t capacity, uint32_t *n_total,
+                                         uint32_t *n_dropped, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!out && capacity > 0) return fail(h, FDAS_ERR_INVALID_ARG, "out is NULL");
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st = sync_set(h, ab);
+  if (st != FDAS_OK) return st;
+  BufferSet &S = h->set[ab];
+  unsigned ctrl[kCtrlWords];
+  CK(h, cudaMemcpy(ctrl, S.d_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
+  uint32_t total = 0, dropped = 0, written = 0;
+  std::vector<unsigned long long> keys;
+  std::vector<float> pwrs;
+  for (int pl = 0; pl < h->P; ++pl) {
+    const unsigned cnt = ctrl[kCtrlCount + pl];
+    const unsigned kept = std::min(cnt, (unsigned)h->cap);
+    total += cnt;
+    dropped += cnt - kept;
+    if (kept == 0 || written >= capacity) continue;
+    keys.resize(kept);
+    pwrs.resize(kept);
+    CK(h, cudaMemcpy(keys.data(), S.d_key + (size_t)pl * h->cap, sizeof(unsigned long long) * kept,
+                     cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpy(pwrs.data(), S.d_pwr + (size_t)pl * h->cap, sizeof(float) * kept, cudaMemcpyDeviceToHost));
+    for (unsigned i = 0; i < kept && written < capacity; ++i) {
+      fdas_candidate &c = out[written++];
+      c.harmonic = (uint32_t)pl + 1;
+      c.template_num = (int32_t)(keys[i] >> 32) - h->H;
+      c.bin = (uint32_t)(keys[i] & 0xffffffffu);
+      c.power = pwrs[i];
+    }
+  }
+  if (n_total) *n_total = total;
+  if (n_dropped) *n_dropped = dropped;
+  return FDAS_OK;
+}
+
+fdas_status fdas_get_stage_times(fdas_handle *h, fdas_buffer_set ab, float *ms6) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!ms6) return fail(h, FDAS_ERR_INVALID_ARG, "ms6 is NULL");
+  BufferSet &S = h->set[ab];
+  CK(h, cudaSetDevice(h->cfg.device));
+  CK(h, cudaEventSynchronize(S.ev[5]));
+  ms6[0] = elapsed(S.ev[0], S.ev[1]);
+  ms6[1] = elapsed(S.ev[1], S.ev[2]);
+  ms6[2] = elapsed(S.ev[2], S.ev[3]);
+  ms6[3] = elapsed(S.ev[3], S.ev[4]);
+  ms6[4] = elapsed(S.ev[4], S.ev[5]);
+  ms6[5] = elapsed(S.ev[0], S.ev[5]);
+  return FDAS_OK;
+}
+
+void fdas_print_stats(fdas_handle *h, fdas_buffer_set ab, int reset) {
+  if (!h || !valid_set(ab)) return;
+  BufferSet &S = h->set[ab];
+  if (cudaEventSynchronize(S.ev[5]) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  if (reset || !h->pipeline_start) {
+    if (!h->pipeline_start) cudaEventCreate(&h->pipeline_start);
+    // FDAS.cpp:643-666 measures from the first input transfer of the series
+    cudaEventRecord(h->pipeline_start, S.stream);
+    cudaEventSynchronize(h->pipeline_start);
+    h->pipeline_accum_ms = 0.f;
+    h->pipeline_launches = 1;
+  } else {
+    ++h->pipeline_launches;
+  }
+  const char set_c = ab == FDAS_SET_A ? 'A' : 'B';
+  logf(h, "[INFO] Launch  #%u%c complete", h->pipeline_launches, set_c);
+  logf(h, "[INFO]   Preparation duration: %.3f ms", elapsed(S.ev[1], S.ev[2]));
+  logf(h, "[INFO]   FT convolution and IFFT duration: %.3f ms", elapsed(S.ev[2], S.ev[3]));
+  logf(h, "[INFO]   Harmonic summing duration: %.3f ms", elapsed(S.ev[3], S.ev[4]));
+  logf(h, "[INFO]   Total duration: %.3f ms", elapsed(S.ev[0], S.ev[5]));
+}
+
+void fdas_print_events(fdas_handle *h, fdas_buffer_set ab) {
+  if (!h || !valid_set(ab)) return;
+  BufferSet &S = h->set[ab];
+  if (cudaEventSynchronize(S.ev[5]) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  // FDAS.cpp:668-686: "@@@" line of stage boundaries, here in microseconds
+  // relative to the input transfer start
+  logf(h, "@@@,%c,0,%.1f,%.1f,%.1f,%.1f,%.1f", ab == FDAS_SET_A ? 'A' : 'B', 1e3f * elapsed(S.ev[0], S.ev[1]),
+       1e3f * elapsed(S.ev[0], S.ev[2]), 1e3f * elapsed(S.ev[0], S.ev[3]), 1e3f * elapsed(S.ev[0], S.ev[4]),
+       1e3f * elapsed(S.ev[0], S.ev[5]));
+}
+
+void fdas_set_log(fdas_handle *h, fdas_log_fn fn, void *user) {
+  if (!h) return;
+  h->log_fn = fn;
+  h->log_user = user;
+}
+
+uint32_t fdas_get_input_sz(const fdas_handle *h) { return h ? (uint32_t)h->N : 0; }
+uint32_t fdas_get_tiles_sz(const fdas_handle *h) { return h ? (uint32_t)(h->n_tiles * kTile) : 0; }
+uint32_t fdas_get_templates_sz(const fdas_handle *h) { return h ? (uint32_t)(h->T * kTile) : 0; }
+uint32_t fdas_get_thresholds_sz(const fdas_handle *h) { return h ? (uint32_t)h->P : 0; }
+uint32_t fdas_get_fop_sz(const fdas_handle *h) { return h ? (uint32_t)((size_t)h->T * h->N) : 0; }
+uint32_t fdas_get_candidate_list_sz(const fdas_handle *h) { return h ? (uint32_t)(h->P * h->per_plane) : 0; }
+
+fdas_status fdas_host_alloc(void **ptr, size_t bytes) {
+  if (!ptr) return fail(nullptr, FDAS_ERR_INVALID_ARG, "ptr is NULL");
+  cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaHostAlloc", __FILE__, __LINE__);
+  return FDAS_OK;
+}
+void fdas_host_free(void *ptr) {
+  if (ptr) cudaFreeHost(ptr);
+}
+fdas_status fdas_host_register(void *ptr, size_t bytes) {
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaHostRegister", __FILE__, __LINE__);
+  return FDAS_OK;
+}
+fdas_status fdas_host_unregister(void *ptr) {
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaHostUnregister", __FILE__, __LINE__);
+  return FDAS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,319 @@
+// Warp-level 2048-point complex FFT for sm_103a.
+//
+// One warp computes one 2048-point transform: each of the 32 lanes holds 64
+// complex values in registers.  The transform is split as 2048 = 64 x 32 with
+// a single shared-memory exchange:
+//
+//   inverse (sign +1), input Y[k] in natural order, k = 32 k' + kappa:
+//     pass 1  lane kappa:  Z_kappa[m] = DFT64_k'( Y[32 k' + kappa] )      m in [0,64)
+//     twiddle             V_kappa[m] = Z_kappa[m] * w^(m kappa),  w = e^(+2 pi i / 2048)
+//     exchange            lane l gets V_kappa[l], V_kappa[l + 32] for all kappa
+//     pass 2  lane l:     y[m + 64 d] = DFT32_kappa( V_kappa[m] ),  m in {l, l+32}
+//   so lane l ends with outputs n = l + 32 c + 64 d (c in {0,1}, d in [0,32)):
+//   for fixed (c, d) the 32 lanes hold 32 consecutive outputs.
+//
+//   forward (sign -1) is the mirror image: natural-order input x[m + 64 d] is
+//   loaded with lane l holding m in {l, l+32}; DFT32 over d, twiddle
+//   w^(-m kappa), exchange, DFT64 over m; lane kappa ends with X[32 k' + kappa].
+//
+// Global loads and stores of both directions are therefore unit-stride across
+// the warp, which makes every access coalesced without any permutation of the
+// spectra in memory.  The FPGA reference uses a radix-2^2 streaming engine with
+// bit-reversed output instead (fft_4p.cl); only the transform is shared.
+//
+// Small DFTs (4, 8, 32 = 4x8, 64 = 8x8) are fully unrolled with compile-time
+// twiddle constants (template variables evaluated by the host compiler), so
+// trivial rotations cost no multiplies.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <utility>
+#include <type_traits>
+
+namespace fdas {
+
+// ---------------------------------------------------------------- constants
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+// cos / sin by Taylor series after reduction to [-pi/4, pi/4]; only ever
+// evaluated by the host compiler when initialising constexpr template
+// variables below.
+constexpr double taylor_cos(double x) {
+  double s = 0, t = 1;
+  for (int i = 0; i < 24; ++i) { s += t; t *= -x * x / ((2.0 * i + 1) * (2.0 * i + 2)); }
+  return s;
+}
+constexpr double taylor_sin(double x) {
+  double s = 0, t = x;
+  for (int i = 0; i < 24; ++i) { s += t; t *= -x * x / ((2.0 * i + 2) * (2.0 * i + 3)); }
+  return s;
+}
+// cos(2 pi j / n), sin(2 pi j / n) for integer j, n using octant symmetry
+constexpr double cexpr_cos_frac(long j, long n) {
+  j = ((j % n) + n) % n;
+  // reduce to the first octant with exact integer arithmetic on 8 j / n
+  long e = 8 * j;  // angle in units of (2 pi / 8n)
+  long oct = e / n;
+  long rem = e - oct * n;  // angle = (oct + rem/n) * pi/4
+  double a = (kTwoPi / 8.0) * (double)rem / (double)n;
+  double b = (kTwoPi / 8.0) - a;
+  switch (oct) {
+    case 0: return taylor_cos(a);
+    case 1: return taylor_sin(b);
+    case 2: return -taylor_sin(a);
+    case 3: return -taylor_cos(b);
+    case 4: return -taylor_cos(a);
+    case 5: return -taylor_sin(b);
+    case 6: return taylor_sin(a);
+    default: return taylor_cos(b);
+  }
+}
+constexpr double cexpr_sin_frac(long j, long n) { return cexpr_cos_frac(j - n / 4, n) ; }
+
+template <int N, int J> constexpr float kCos = (float)cexpr_cos_frac(J, N);
+template <int N, int J> constexpr float kSin = (float)cexpr_sin_frac(J, N);
+constexpr float kRsqrt2 = 0.70710678118654752440f;
+
+// ------------------------------------------------------------ static for
+template <typename F, int... I>
+__device__ __forceinline__ void sfor_impl(F &&f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void sfor(F &&f) {
+  sfor_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+// ------------------------------------------------------------ complex ops
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// v * e^(S i 2 pi J / N) with compile-time S, N, J.  Rotations by multiples of
+// pi/4 use the cheap forms.
+template <int S, int N, int J>
+__device__ __forceinline__ float2 rot(float2 v) {
+  constexpr int j = ((J % N) + N) % N;
+  if constexpr (j == 0) {
+    return v;
+  } else if constexpr (2 * j == N) {
+    return make_float2(-v.x, -v.y);
+  } else if constexpr (4 * j == N) {  // * (S i)
+    return S > 0 ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
+  } else if constexpr (4 * j == 3 * N) {  // * (-S i)
+    return S > 0 ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
+  } else if constexpr (8 * j == N) {  // r (1 + S i)
+    return S > 0 ? make_float2(kRsqrt2 * (v.x - v.y), kRsqrt2 * (v.y + v.x))
+                 : make_float2(kRsqrt2 * (v.x + v.y), kRsqrt2 * (v.y - v.x));
+  } else if constexpr (8 * j == 3 * N) {  // r (-1 + S i)
+    return S > 0 ? make_float2(-kRsqrt2 * (v.x + v.y), kRsqrt2 * (v.x - v.y))
+                 : make_float2(kRsqrt2 * (v.y - v.x), -kRsqrt2 * (v.x + v.y));
+  } else if constexpr (8 * j == 5 * N) {  // r (-1 - S i)
+    return S > 0 ? make_float2(kRsqrt2 * (v.y - v.x), -kRsqrt2 * (v.x + v.y))
+                 : make_float2(-kRsqrt2 * (v.x + v.y), kRsqrt2 * (v.x - v.y));
+  } else if constexpr (8 * j == 7 * N) {  // r (1 - S i)
+    return S > 0 ? make_float2(kRsqrt2 * (v.x + v.y), kRsqrt2 * (v.y - v.x))
+                 : make_float2(kRsqrt2 * (v.x - v.y), kRsqrt2 * (v.y + v.x));
+  } else {
+    constexpr float c = kCos<N, j>;
+    constexpr float s = S * kSin<N, j>;
+    return make_float2(fmaf(v.x, c, -v.y * s), fmaf(v.x, s, v.y * c));
+  }
+}
+
+// ------------------------------------------------------------ small DFTs
+// In-place DFTs on v[OFF + STRIDE * i]; outputs in natural order.
+template <int S, int OFF, int STRIDE>
+__device__ __forceinline__ void dft2(float2 *v) {
+  float2 a = v[OFF], b = v[OFF + STRIDE];
+  v[OFF] = cadd(a, b);
+  v[OFF + STRIDE] = csub(a, b);
+}
+
+template <int S, int OFF, int STRIDE>
+__device__ __forceinline__ void dft4(float2 *v) {
+  float2 x0 = v[OFF], x1 = v[OFF + STRIDE], x2 = v[OFF + 2 * STRIDE], x3 = v[OFF + 3 * STRIDE];
+  float2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3);
+  float2 t3 = rot<S, 4, 1>(csub(x1, x3));
+  v[OFF] = cadd(t0, t2);
+  v[OFF + 2 * STRIDE] = csub(t0, t2);
+  v[OFF + STRIDE] = cadd(t1, t3);
+  v[OFF + 3 * STRIDE] = csub(t1, t3);
+}
+
+template <int S, int OFF, int STRIDE>
+__device__ __forceinline__ void dft8(float2 *v) {
+  // radix-2 decimation in time: two DFT4 on even / odd inputs
+  float2 e[4] = {v[OFF], v[OFF + 2 * STRIDE], v[OFF + 4 * STRIDE], v[OFF + 6 * STRIDE]};
+  float2 o[4] = {v[OFF + STRIDE], v[OFF + 3 * STRIDE], v[OFF + 5 * STRIDE], v[OFF + 7 * STRIDE]};
+  dft4<S, 0, 1>(e);
+  dft4<S, 0, 1>(o);
+  float2 o1 = rot<S, 8, 1>(o[1]), o2 = rot<S, 8, 2>(o[2]), o3 = rot<S, 8, 3>(o[3]);
+  v[OFF] = cadd(e[0], o[0]);
+  v[OFF + 4 * STRIDE] = csub(e[0], o[0]);
+  v[OFF + STRIDE] = cadd(e[1], o1);
+  v[OFF + 5 * STRIDE] = csub(e[1], o1);
+  v[OFF + 2 * STRIDE] = cadd(e[2], o2);
+  v[OFF + 6 * STRIDE] = csub(e[2], o2);
+  v[OFF + 3 * STRIDE] = cadd(e[3], o3);
+  v[OFF + 7 * STRIDE] = csub(e[3], o3);
+}
+
+template <int S, int R, int OFF, int STRIDE>
+__device__ __forceinline__ void dft_small(float2 *v) {
+  if constexpr (R == 2) dft2<S, OFF, STRIDE>(v);
+  else if constexpr (R == 4) dft4<S, OFF, STRIDE>(v);
+  else dft8<S, OFF, STRIDE>(v);
+}
+
+// Composite DFT of size R1*R2 on v[OFF + STRIDE * n] (n natural order).
+// Output X[k1 + R1 k2] is left in v[OFF + STRIDE * (R2 k1 + k2)].
+template <int S, int R1, int R2, int OFF, int STRIDE>
+__device__ __forceinline__ void dft_composite(float2 *v) {
+  constexpr int N = R1 * R2;
+  // step 1: R2 DFTs of size R1 over n1 (n = R2 n1 + n2)
+  sfor<R2>([&](auto N2) {
+    constexpr int n2 = decltype(N2)::value;
+    dft_small<S, R1, OFF + STRIDE * n2, STRIDE * R2>(v);
+  });
+  // step 2: internal twiddles w_N^(n2 k1)
+  sfor<R1>([&](auto K1) {
+    constexpr int k1 = decltype(K1)::value;
+    sfor<R2>([&](auto N2) {
+      constexpr int n2 = decltype(N2)::value;
+      constexpr int idx = OFF + STRIDE * (R2 * k1 + n2);
+      v[idx] = rot<S, N, n2 * k1>(v[idx]);
+    });
+  });
+  // step 3: R1 DFTs of size R2 over n2
+  sfor<R1>([&](auto K1) {
+    constexpr int k1 = decltype(K1)::value;
+    dft_small<S, R2, OFF + STRIDE * R2 * k1, STRIDE>(v);
+  });
+}
+
+// Register slot of output k for the 64 = 8x8 and 32 = 4x8 transforms.
+__host__ __device__ constexpr int pos64(int k) { return 8 * (k % 8) + k / 8; }
+__host__ __device__ constexpr int pos32(int k) { return 8 * (k % 4) + k / 4; }
+
+template <int S, int OFF>
+__device__ __forceinline__ void dft64(float2 *v) { dft_composite<S, 8, 8, OFF, 1>(v); }
+template <int S, int OFF>
+__device__ __forceinline__ void dft32(float2 *v) { dft_composite<S, 4, 8, OFF, 1>(v); }
+
+// ------------------------------------------------------------ exchange
+// Shared-memory buffer of one warp: 32 rows (kappa) x 64 columns (m), row
+// pitch 66 complex values: 16-byte row starts and conflict-free access for
+// both the 8-byte column-wise and 16-byte row-wise patterns below.
+constexpr int kExPitch = 66;
+constexpr int kExFloats = 32 * kExPitch * 2;  // floats per warp
+
+// Per-lane twiddle bases for w^(m * lane), m = mlo + 8 mhi:
+//   lo[j] = w^(j lane), hi[j] = w^(8 j lane), j in [0, 8).
+// ``table`` holds e^(i 2 pi j / 2048), j in [0, 2048) (sign applied here).
+struct TwiddleBases {
+  float2 lo[8];
+  float2 hi[8];
+};
+
+template <int S>
+__device__ __forceinline__ TwiddleBases load_twiddle_bases(const float2 *__restrict__ table, int lane) {
+  TwiddleBases tb;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float2 a = __ldg(table + ((j * lane) & 2047));
+    float2 b = __ldg(table + ((8 * j * lane) & 2047));
+    tb.lo[j] = make_float2(a.x, S * a.y);
+    tb.hi[j] = make_float2(b.x, S * b.y);
+  }
+  return tb;
+}
+
+// Inverse transform core: v[64] holds Y[32 k' + lane] at v[k'] on entry.  On
+// exit v[32 c + pos32(d)] holds y[lane + 32 c + 64 d].  ``ex`` is this warp's
+// exchange buffer (kExFloats floats, 16-byte aligned).
+__device__ __forceinline__ void ifft2048_core(float2 *v, const TwiddleBases &tb, float *ex, int lane) {
+  dft64<+1, 0>(v);
+  // twiddle V[m] = Z[m] w^(m lane);  Z[m] sits at v[pos64(m)] = v[8 mlo + mhi]
+  sfor<8>([&](auto MLO) {
+    constexpr int mlo = decltype(MLO)::value;
+    sfor<8>([&](auto MHI) {
+      constexpr int mhi = decltype(MHI)::value;
+      constexpr int idx = 8 * mlo + mhi;
+      if constexpr (mlo == 0 && mhi == 0) {
+      } else if constexpr (mlo == 0) {
+        v[idx] = cmul(v[idx], tb.hi[mhi]);
+      } else if constexpr (mhi == 0) {
+        v[idx] = cmul(v[idx], tb.lo[mlo]);
+      } else {
+        v[idx] = cmul(v[idx], cmul(tb.lo[mlo], tb.hi[mhi]));
+      }
+    });
+  });
+  // exchange: row = lane (kappa), column m; 16-byte stores of (m, m+1)
+  float4 *row = reinterpret_cast<float4 *>(ex + 2 * kExPitch * lane);
+  sfor<32>([&](auto P) {
+    constexpr int p = decltype(P)::value;  // m = 2p, 2p+1
+    float2 a = v[pos64(2 * p)], b = v[pos64(2 * p + 1)];
+    row[p] = make_float4(a.x, a.y, b.x, b.y);
+  });
+  __syncwarp();
+  const float2 *col = reinterpret_cast<const float2 *>(ex);
+  sfor<2>([&](auto C) {
+    constexpr int c = decltype(C)::value;
+    sfor<32>([&](auto K) {
+      constexpr int kap = decltype(K)::value;
+      v[32 * c + kap] = col[kExPitch * kap + lane + 32 * c];
+    });
+  });
+  __syncwarp();
+  dft32<+1, 0>(v);
+  dft32<+1, 32>(v);
+}
+
+// Forward transform core: v[32 c + d] holds x[lane + 32 c + 64 d] on entry.
+// On exit v[pos64(k')] holds X[32 k' + lane].
+__device__ __forceinline__ void fft2048_core(float2 *v, const TwiddleBases &tb, float *ex, int lane) {
+  dft32<-1, 0>(v);
+  dft32<-1, 32>(v);
+  // twiddle: U_m[kappa] * w^(-m kappa), m = lane + 32 c, kappa = klo + 8 khi.
+  // w^(-(lane + 32c) kappa) = w^(-lane kappa) * e^(-2 pi i c kappa / 64)
+  // per-lane part from the bases: kappa = klo + 8 khi -> lo[klo] * hi[khi]
+  sfor<2>([&](auto C) {
+    constexpr int c = decltype(C)::value;
+    sfor<32>([&](auto K) {
+      constexpr int kap = decltype(K)::value;
+      constexpr int klo = kap % 8, khi = kap / 8;
+      constexpr int idx = 32 * c + pos32(kap);
+      float2 t = v[idx];
+      if constexpr (klo != 0 && khi != 0) t = cmul(t, cmul(tb.lo[klo], tb.hi[khi]));
+      else if constexpr (klo != 0) t = cmul(t, tb.lo[klo]);
+      else if constexpr (khi != 0) t = cmul(t, tb.hi[khi]);
+      if constexpr (c == 1) t = rot<-1, 64, kap>(t);
+      v[idx] = t;
+    });
+  });
+  // exchange: column writes (8-byte), row reads (16-byte)
+  float2 *col = reinterpret_cast<float2 *>(ex);
+  sfor<2>([&](auto C) {
+    constexpr int c = decltype(C)::value;
+    sfor<32>([&](auto K) {
+      constexpr int kap = decltype(K)::value;
+      col[kExPitch * kap + lane + 32 * c] = v[32 * c + pos32(kap)];
+    });
+  });
+  __syncwarp();
+  const float4 *row = reinterpret_cast<const float4 *>(ex + 2 * kExPitch * lane);
+  sfor<32>([&](auto P) {
+    constexpr int p = decltype(P)::value;
+    float4 q = row[p];
+    v[2 * p] = make_float2(q.x, q.y);
+    v[2 * p + 1] = make_float2(q.z, q.w);
+  });
+  __syncwarp();
+  dft64<-1, 0>(v);
+}
+
+}  // namespace fdas

@@ -1,0 +1,136 @@
+// Kernel parameter blocks and launchers of the FDAS hot path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fdas {
+
+constexpr int kTile = 2048;          // FFT / tile size (gen_info.h:33, 42)
+constexpr int kMaxPlanes = 16;       // harmonic planes supported by the kernels
+constexpr int kHsBins = 256;         // bins per harmonic-summing CTA
+constexpr int kHsThreads = 256;
+constexpr int kSortCap = 8192;       // per-plane candidate capacity (one-CTA sort)
+
+// device status bits (per buffer set)
+constexpr int kStatusHsumTimeout = 1;
+constexpr int kStatusRecheckOverflow = 2;
+
+// ---- (a) overlap-save tiling + forward FFT (tile_input.cl.mako, fft_4p.cl)
+struct TileParams {
+  const float2 *input;    // N spectrum bins
+  int n_bins;
+  int n_tiles;
+  int overlap;            // O
+  int payload;            // P = 2048 - O
+  float2 *tiles;          // n_tiles x 2048, natural bin order
+  const float2 *twiddle;  // e^(+2 pi i j / 2048), j < 2048
+};
+
+// ---- (c) template multiply + inverse FFT + |.|^2 + discard (mux_and_mult,
+//      square_and_discard)
+struct FtcParams {
+  const float2 *tiles;    // n_tiles x 2048
+  const float2 *tmpl;     // n_templates x 2048 spectra, natural order, scaled by 2^-11
+  float *fop;             // n_templates x stride
+  long long fop_stride;
+  int n_bins;
+  int n_tiles;
+  int overlap;
+  int payload;
+  int row_begin;          // first FOP row of the part
+  int n_rows;             // rows of the part
+  const float2 *twiddle;
+};
+
+// ---- (d) harmonic summing + thresholds + candidate compaction (preload,
+//      delay, detect, store_cands; hms_baseline.cl.mako)
+struct HsumParams {
+  const float *fop;
+  long long stride;
+  int n_bins;
+  int half;               // n_templates / 2: row of template t is half + t
+  int n_planes;
+  int tlo[2];             // first |t| of the negative / positive half; > half disables it
+  float trig[kMaxPlanes]; // fast-path trigger: a cell needs a closer look if HP >= trig
+  float hi[kMaxPlanes];   // candidate if HP > hi
+  float lo[kMaxPlanes];   // recheck if lo <= HP <= hi (lo = +inf: never)
+  int sw[kMaxPlanes + 1];   // staged row width (floats) of plane j
+  int soff[kMaxPlanes + 1]; // offset (floats) of plane j's staging block
+  int srows[kMaxPlanes + 1];// rows staged for plane j (= half / j + 1)
+  unsigned stage_bytes;   // total bytes moved by the bulk copies
+  int smem_floats;        // staging floats (after the 16-byte barrier slot)
+  unsigned long long *cand_key;  // [plane][cap] : (row << 32) | bin
+  float *cand_pwr;               // [plane][cap]
+  unsigned *cand_count;          // [plane]
+  int cand_cap;
+  uint4 *rc_list;         // recheck entries (plane, row, bin, 0)
+  unsigned *rc_count;
+  int rc_cap;
+  int *status;
+  long long timeout_ns;   // bound on every wait
+};
+
+// ---- FP64 recheck of near-threshold cells
+struct RecheckParams {
+  const float2 *input;    // the spectrum the FOP was computed from
+  int n_bins;
+  int half;
+  const double2 *taps;    // n_templates x tap_pitch time-domain taps (FP64)
+  const int *tap_len;     // taps per template
+  int tap_pitch;
+  double thr[kMaxPlanes];
+  const uint4 *rc_list;
+  const unsigned *rc_count;
+  int rc_cap;
+  unsigned long long *cand_key;
+  float *cand_pwr;
+  unsigned *cand_count;
+  int cand_cap;
+  int *status;
+};
+
+// ---- sort + fixed-size list
+struct FinalizeParams {
+  unsigned long long *cand_key;
+  float *cand_pwr;
+  const unsigned *cand_count;
+  int cand_cap;
+  int per_plane;          // entries per plane in the fixed-size list
+  uint32_t *compat_loc;   // [plane][per_plane]
+  float *compat_pwr;
+  uint32_t invalid_location;
+};
+
+// ---- template spectra / taps in FP64
+struct SpectraParams {
+  const double2 *taps;    // n_templates x tap_pitch
+  const int *tap_len;
+  int tap_pitch;
+  int n_templates;
+  const double2 *twiddle64;  // e^(-2 pi i j / 2048)
+  float2 *spectra;        // n_templates x 2048, natural, scaled by 2^-11
+};
+
+struct TapsParams {
+  const float2 *spectra;  // n_templates x 2048 natural, unscaled
+  int n_templates;
+  int n_taps;             // taps to recover per template
+  const double2 *twiddle64;
+  double2 *taps;          // n_templates x tap_pitch
+  int *tap_len;
+  int tap_pitch;
+};
+
+cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s);
+cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s);
+cudaError_t launch_hsum(const HsumParams &p, cudaStream_t s);
+cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s);
+cudaError_t launch_finalize(const FinalizeParams &p, int n_planes, cudaStream_t s);
+cudaError_t launch_spectra(const SpectraParams &p, cudaStream_t s);
+cudaError_t launch_taps(const TapsParams &p, cudaStream_t s);
+
+// shared memory bytes needed by launch_hsum for a given plane geometry
+int hsum_smem_bytes(const HsumParams &p);
+
+}  // namespace fdas

@@ -1,0 +1,151 @@
+// (a) overlap-save tiling + forward FFT, (c) fused template multiply,
+// inverse FFT, power and overlap discard, and the FP64 template precompute.
+#include "fft2048.cuh"
+#include "kernels.cuh"
+
+namespace fdas {
+
+constexpr int kWarpsPerCta = 8;
+
+// One warp per tile.  Tile i covers spectrum bins [i P - O, i P + P): bins
+// below 0 (the first tile's overlap) and from N on (the last tile's padding)
+// read as zero -- tile_input.cl.mako:42-94 / ft_conv.py:165-180.
+__global__ void __launch_bounds__(256) tile_fft_kernel(TileParams p) {
+  extern __shared__ float4 smem_f4[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.x * kWarpsPerCta + warp;
+  if (tile >= p.n_tiles) return;
+  float *ex = reinterpret_cast<float *>(smem_f4) + warp * kExFloats;
+  const TwiddleBases tb = load_twiddle_bases<-1>(p.twiddle, lane);
+  float2 v[64];
+  const long long start = (long long)tile * p.payload - p.overlap;
+  sfor<2>([&](auto C) {
+    constexpr int c = decltype(C)::value;
+    sfor<32>([&](auto D) {
+      constexpr int d = decltype(D)::value;
+      const long long b = start + lane + 32 * c + 64 * d;
+      v[32 * c + d] = (b >= 0 && b < p.n_bins) ? __ldg(p.input + b) : make_float2(0.f, 0.f);
+    });
+  });
+  fft2048_core(v, tb, ex, lane);
+  float2 *out = p.tiles + (long long)tile * kTile;
+  sfor<64>([&](auto K) {
+    constexpr int k = decltype(K)::value;
+    out[32 * k + lane] = v[pos64(k)];
+  });
+}
+
+// One warp per (tile, template).  Y = S_tile * T_tmpl (templates carry the
+// 1/2048 of the inverse transform, so |y|^2 already includes the reference's
+// power normalisation by 2048^2, utils.cl.mako:41-47); y = IFFT(Y);
+// FOP[row][i P + n - O] = |y[n]|^2 for n >= O, trimmed to N bins
+// (square_and_discard.cl.mako:28-76).
+__global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
+  extern __shared__ float4 smem_f4[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.x;
+  const int rloc = blockIdx.y * kWarpsPerCta + warp;
+  if (rloc >= p.n_rows) return;
+  const int row = p.row_begin + rloc;
+  float *ex = reinterpret_cast<float *>(smem_f4) + warp * kExFloats;
+  const TwiddleBases tb = load_twiddle_bases<+1>(p.twiddle, lane);
+  const float2 *s = p.tiles + (long long)tile * kTile + lane;
+  const float2 *t = p.tmpl + (long long)row * kTile + lane;
+  float2 v[64];
+  sfor<64>([&](auto K) {
+    constexpr int k = decltype(K)::value;
+    v[k] = cmul(__ldg(s + 32 * k), __ldg(t + 32 * k));
+  });
+  ifft2048_core(v, tb, ex, lane);
+  float *out = p.fop + (long long)row * p.fop_stride;
+  const long long base = (long long)tile * p.payload - p.overlap;
+  sfor<2>([&](auto C) {
+    constexpr int c = decltype(C)::value;
+    sfor<32>([&](auto D) {
+      constexpr int d = decltype(D)::value;
+      const int n = lane + 32 * c + 64 * d;
+      const long long b = base + n;
+      const float2 y = v[32 * c + pos32(d)];
+      if (n >= p.overlap && b < p.n_bins) out[b] = fmaf(y.x, y.x, y.y * y.y);
+    });
+  });
+}
+
+// FP64 DFT of the time-domain taps -> float spectra scaled by 2^-11.
+__global__ void spectra_kernel(SpectraParams p) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (k >= kTile || r >= p.n_templates) return;
+  const double2 *h = p.taps + (long long)r * p.tap_pitch;
+  const int len = p.tap_len[r];
+  double re = 0.0, im = 0.0;
+  for (int q = 0; q < len; ++q) {
+    const double2 w = p.twiddle64[(q * k) & (kTile - 1)];
+    const double2 x = h[q];
+    re += x.x * w.x - x.y * w.y;
+    im += x.x * w.y + x.y * w.x;
+  }
+  const double scale = 1.0 / 2048.0;
+  p.spectra[(long long)r * kTile + k] = make_float2((float)(re * scale), (float)(im * scale));
+}
+
+// FP64 inverse DFT of float spectra -> the first n_taps time-domain taps.
+__global__ void taps_kernel(TapsParams p) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (r >= p.n_templates) return;
+  if (q == 0) p.tap_len[r] = p.n_taps;
+  if (q >= p.n_taps) return;
+  const float2 *sp = p.spectra + (long long)r * kTile;
+  double re = 0.0, im = 0.0;
+  for (int k = 0; k < kTile; ++k) {
+    const double2 w = p.twiddle64[(q * k) & (kTile - 1)];  // e^(-i..): use conjugate
+    const float2 x = sp[k];
+    re += (double)x.x * w.x + (double)x.y * w.y;
+    im += (double)x.y * w.x - (double)x.x * w.y;
+  }
+  p.taps[(long long)r * p.tap_pitch + q] = make_double2(re / 2048.0, im / 2048.0);
+}
+
+static int ex_smem_bytes() { return kWarpsPerCta * kExFloats * (int)sizeof(float); }
+
+cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s) {
+  static bool attr = false;
+  const int smem = ex_smem_bytes();
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tile_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((p.n_tiles + kWarpsPerCta - 1) / kWarpsPerCta);
+  tile_fft_kernel<<<grid, 256, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
+  static bool attr = false;
+  const int smem = ex_smem_bytes();
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(ftc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  if (p.n_rows <= 0 || p.n_tiles <= 0) return cudaSuccess;
+  dim3 grid(p.n_tiles, (p.n_rows + kWarpsPerCta - 1) / kWarpsPerCta);
+  ftc_kernel<<<grid, 256, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spectra(const SpectraParams &p, cudaStream_t s) {
+  dim3 grid(kTile / 128, p.n_templates);
+  spectra_kernel<<<grid, 128, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_taps(const TapsParams &p, cudaStream_t s) {
+  dim3 grid((p.n_taps + 127) / 128, p.n_templates);
+  taps_kernel<<<grid, 128, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace fdas

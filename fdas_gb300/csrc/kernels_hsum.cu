@@ -1,0 +1,386 @@
+// (d) harmonic summing, thresholding and candidate compaction; FP64 recheck of
+// near-threshold cells; per-plane sort and the fixed-size candidate list.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include <utility>
+#include <type_traits>
+
+#include "kernels.cuh"
+
+namespace fdas {
+
+template <typename F, int... I>
+__device__ __forceinline__ void hs_sfor_impl(F &&f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void hs_sfor(F &&f) {
+  hs_sfor_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return done != 0;
+}
+// TMA bulk copy global -> shared, completion signalled on the mbarrier
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait on phase 0 of the barrier; false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, long long timeout_ns) {
+  if (mbar_try_wait(bar, 0)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (true) {
+    if (mbar_try_wait(bar, 0)) return true;
+    if ((long long)(globaltimer_ns() - t0) > timeout_ns) return false;
+  }
+}
+
+// warp-aggregated append of one record to plane `plane`'s list
+__device__ __forceinline__ void append_candidate(const HsumParams &p, int plane, int row, int bin, float pwr) {
+  const unsigned active = __activemask();
+  const unsigned peers = __match_any_sync(active, plane);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(p.cand_count + plane, (unsigned)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  const unsigned idx = base + __popc(peers & ((1u << lane) - 1u));
+  if (idx < (unsigned)p.cand_cap) {
+    const long long o = (long long)plane * p.cand_cap + idx;
+    p.cand_key[o] = ((unsigned long long)(unsigned)row << 32) | (unsigned)bin;
+    p.cand_pwr[o] = pwr;
+  }
+}
+
+__device__ __forceinline__ void append_recheck(const HsumParams &p, int plane, int row, int bin) {
+  const unsigned idx = atomicAdd(p.rc_count, 1u);
+  if (idx < (unsigned)p.rc_cap) p.rc_list[idx] = make_uint4((unsigned)plane, (unsigned)row, (unsigned)bin, 0u);
+  else atomicOr(p.status, kStatusRecheckOverflow);
+}
+
+// One CTA per (256-bin block, sign half).  Warp w handles the templates
+// |t| = tlo + w + 8k of the half; lane l the bins f0 + 4 l + 128 i + e
+// (i < 2, e < 4).  For plane j >= 2 the rows trunc(t / j) and bins
+// [f0/j, (f0+255)/j] of the half are staged in shared memory by TMA bulk
+// copies; plane 1 is read straight from global memory.
+//
+// HP_1 = FOP[t][f], HP_j = HP_{j-1} + FOP[trunc(t/j)][f/j] accumulated in FP32
+// in this order -- hsum.py:95-120 / hms_baseline.cl.mako:55-84 -- so the
+// values match hsum.py bit for bit for the same FOP.  A cell is a candidate of
+// plane j if HP_j > thr_j (strict, hsum.py:134 / detect.cl.mako:185).
+template <int MAXP>
+__global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
+  extern __shared__ __align__(128) float hs_smem[];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(hs_smem);
+  float *stage = hs_smem + 4;
+  const int halfsel = blockIdx.y;
+  const int sgn = halfsel ? 1 : -1;
+  const int tlo = p.tlo[halfsel];
+  const int H = p.half;
+  if (tlo > H) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int f0 = blockIdx.x * kHsBins;
+  const int P = p.n_planes;
+  const bool staged = p.stage_bytes > 0;
+
+  if (staged) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (warp == 0) {
+      if (lane == 0) mbar_arrive_expect_tx(bar, p.stage_bytes);
+      __syncwarp();
+      for (int j = 2; j <= P; ++j) {
+        const int a0 = (f0 / j) & ~3;
+        const int w = p.sw[j];
+        for (int r = lane; r < p.srows[j]; r += 32) {
+          const float *src = p.fop + (long long)(H + sgn * r) * p.stride + a0;
+          bulk_g2s(stage + p.soff[j] + r * w, src, (uint32_t)w * 4u, bar);
+        }
+      }
+    }
+  }
+
+  // ---- fast path: accumulate all planes, only flag cells at/above trig
+  constexpr int KMAX = 8;  // rows per warp: ceil(64 / 8) covers half <= 63
+  float acc[KMAX][8];
+  int trow[KMAX];
+  int nk = 0;
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) {
+    trow[k] = tlo + warp + 8 * k;
+    if (trow[k] <= H) nk = k + 1;
+  }
+  bool flag = false;
+  const int fb = f0 + 4 * lane;
+#pragma unroll
+  for (int k = 0; k < KMAX; ++k) {
+    if (k < nk) {
+      const float *rowp = p.fop + (long long)(H + sgn * trow[k]) * p.stride;
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int f = fb + 128 * i;
+        const float4 q = __ldg(reinterpret_cast<const float4 *>(rowp + f));
+        acc[k][4 * i + 0] = (f + 0 < p.n_bins) ? q.x : -CUDART_INF_F;
+        acc[k][4 * i + 1] = (f + 1 < p.n_bins) ? q.y : -CUDART_INF_F;
+        acc[k][4 * i + 2] = (f + 2 < p.n_bins) ? q.z : -CUDART_INF_F;
+        acc[k][4 * i + 3] = (f + 3 < p.n_bins) ? q.w : -CUDART_INF_F;
+      }
+#pragma unroll
+      for (int e = 0; e < 8; ++e) flag |= acc[k][e] >= p.trig[0];
+    }
+  }
+
+  // the timeout decision is made uniform over the CTA before any warp vote
+  bool ok = true;
+  if (staged) ok = __syncthreads_and(mbar_wait_bounded(bar, p.timeout_ns)) != 0;
+  if (!ok) {
+    if (threadIdx.x == 0) atomicOr(p.status, kStatusHsumTimeout);
+    // let copies still in flight land before the CTA exits (bounded again)
+    mbar_wait_bounded(bar, p.timeout_ns);
+    return;
+  }
+
+  hs_sfor<MAXP - 1>([&](auto JJ) {
+    constexpr int j = decltype(JJ)::value + 2;
+    if (j <= P) {
+      const int a0 = (f0 / j) & ~3;
+      int off[8];
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) off[4 * i + e] = (fb + 128 * i + e) / j - a0;
+      const float *blk = stage + p.soff[j];
+      const int w = p.sw[j];
+      const float tj = p.trig[j - 1];
+#pragma unroll
+      for (int k = 0; k < KMAX; ++k) {
+        if (k < nk) {
+          const float *rs = blk + (trow[k] / j) * w;
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            acc[k][e] += rs[off[e]];
+            flag |= acc[k][e] >= tj;
+          }
+        }
+      }
+    }
+  });
+
+  // ---- slow path (rare): recompute flagged lanes' cells in the same order
+  // and emit candidates / recheck entries
+  if (__any_sync(0xffffffffu, flag)) {
+    if (flag) {
+      for (int k = 0; k < nk; ++k) {
+        const int tk = tlo + warp + 8 * k;
+        const int row = H + sgn * tk;
+        const float *rowp = p.fop + (long long)row * p.stride;
+        for (int e8 = 0; e8 < 8; ++e8) {
+          const int f = fb + 128 * (e8 >> 2) + (e8 & 3);
+          if (f >= p.n_bins) continue;
+          float a = rowp[f];
+          for (int j = 1; j <= P; ++j) {
+            if (j > 1) {
+              const int a0 = (f0 / j) & ~3;
+              a += stage[p.soff[j] + (tk / j) * p.sw[j] + f / j - a0];
+            }
+            if (a > p.hi[j - 1]) append_candidate(p, j - 1, row, f, a);
+            else if (a >= p.lo[j - 1]) append_recheck(p, j - 1, row, f);
+          }
+        }
+      }
+    }
+  }
+}
+
+// One warp per recheck entry: HP_j of the cell in FP64 from the spectrum and
+// the FP64 taps, FOP(r, g) = |sum_q X[g - q] h_r[q]|^2 (ft_conv.py:201-205).
+__global__ void __launch_bounds__(256) recheck_kernel(RecheckParams p) {
+  const int lane = threadIdx.x & 31;
+  const unsigned n = min(*p.rc_count, (unsigned)p.rc_cap);
+  const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (unsigned e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
+    const uint4 ent = p.rc_list[e];
+    const int plane = (int)ent.x, row = (int)ent.y, bin = (int)ent.z;
+    const int t = row - p.half;
+    double hp = 0.0;
+    for (int j = 1; j <= plane + 1; ++j) {
+      const int tj = (t >= 0) ? t / j : -((-t) / j);
+      const int r = p.half + tj;
+      const int g = bin / j;
+      const int len = p.tap_len[r];
+      const double2 *h = p.taps + (long long)r * p.tap_pitch;
+      double re = 0.0, im = 0.0;
+      for (int q = lane; q < len && q <= g; q += 32) {
+        const float2 x = p.input[g - q];
+        const double2 c = h[q];
+        re += (double)x.x * c.x - (double)x.y * c.y;
+        im += (double)x.x * c.y + (double)x.y * c.x;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+      }
+      hp += re * re + im * im;
+    }
+    if (lane == 0 && hp > p.thr[plane]) {
+      const unsigned idx = atomicAdd(p.cand_count + plane, 1u);
+      if (idx < (unsigned)p.cand_cap) {
+        const long long o = (long long)plane * p.cand_cap + idx;
+        p.cand_key[o] = ((unsigned long long)(unsigned)row << 32) | (unsigned)bin;
+        p.cand_pwr[o] = (float)hp;
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------- per-plane sort
+struct Rec {
+  unsigned long long key;
+  float pwr;
+};
+
+// ascending by key
+__device__ __forceinline__ bool less_key(const Rec &a, const Rec &b) { return a.key < b.key; }
+// "stronger first": power descending, key ascending on ties
+__device__ __forceinline__ bool less_pwr(const Rec &a, const Rec &b) {
+  return (a.pwr > b.pwr) || (a.pwr == b.pwr && a.key < b.key);
+}
+
+template <bool BY_PWR>
+__device__ void bitonic_sort(unsigned long long *keys, float *pwrs, int m) {
+  for (int k = 2; k <= m; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          Rec a{keys[i], pwrs[i]}, b{keys[ixj], pwrs[ixj]};
+          const bool up = (i & k) == 0;
+          const bool b_less = BY_PWR ? less_pwr(b, a) : less_key(b, a);
+          const bool a_less = BY_PWR ? less_pwr(a, b) : less_key(a, b);
+          if (up ? b_less : a_less) {
+            keys[i] = b.key; pwrs[i] = b.pwr;
+            keys[ixj] = a.key; pwrs[ixj] = a.pwr;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(1024) finalize_kernel(FinalizeParams p) {
+  extern __shared__ __align__(16) unsigned char fz_smem[];
+  const int plane = blockIdx.x;
+  const int n = (int)min(p.cand_count[plane], (unsigned)p.cand_cap);
+  int m = 1;
+  while (m < n) m <<= 1;
+  unsigned long long *keys = reinterpret_cast<unsigned long long *>(fz_smem);
+  float *pwrs = reinterpret_cast<float *>(keys + kSortCap);
+  unsigned long long *gk = p.cand_key + (long long)plane * p.cand_cap;
+  float *gp = p.cand_pwr + (long long)plane * p.cand_cap;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    keys[i] = i < n ? gk[i] : ~0ull;
+    pwrs[i] = i < n ? gp[i] : -CUDART_INF_F;
+  }
+  __syncthreads();
+  if (n > 1) bitonic_sort<false>(keys, pwrs, m);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    gk[i] = keys[i];
+    gp[i] = pwrs[i];
+  }
+  __syncthreads();
+  int kept = n;
+  if (n > p.per_plane) {
+    bitonic_sort<true>(keys, pwrs, m);
+    kept = p.per_plane;
+    // re-sort the kept strongest by location: pad the rest with max keys
+    for (int i = threadIdx.x; i < m; i += blockDim.x)
+      if (i >= kept) { keys[i] = ~0ull; pwrs[i] = -CUDART_INF_F; }
+    __syncthreads();
+    bitonic_sort<false>(keys, pwrs, m);
+  }
+  uint32_t *cl = p.compat_loc + (long long)plane * p.per_plane;
+  float *cp = p.compat_pwr + (long long)plane * p.per_plane;
+  for (int i = threadIdx.x; i < p.per_plane; i += blockDim.x) {
+    if (i < kept) {
+      const unsigned row = (unsigned)(keys[i] >> 32), bin = (unsigned)(keys[i] & 0xffffffffu);
+      // gen_info.h:62-64: ((h-1)&7)<<29 | (row&0x7f)<<22 | (bin&0x3fffff)
+      cl[i] = (((unsigned)plane & 7u) << 29) | ((row & 0x7fu) << 22) | (bin & 0x3fffffu);
+      cp[i] = pwrs[i];
+    } else {
+      cl[i] = p.invalid_location;
+      cp[i] = -1.0f;
+    }
+  }
+}
+
+// ----------------------------------------------------------------- launchers
+int hsum_smem_bytes(const HsumParams &p) { return 16 + p.smem_floats * 4; }
+
+template <int MAXP>
+static cudaError_t launch_hsum_t(const HsumParams &p, cudaStream_t s) {
+  const int smem = hsum_smem_bytes(p);
+  cudaError_t e = cudaFuncSetAttribute(hsum_kernel<MAXP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((p.n_bins + kHsBins - 1) / kHsBins, 2);
+  hsum_kernel<MAXP><<<grid, kHsThreads, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hsum(const HsumParams &p, cudaStream_t s) {
+  if (p.n_planes <= 4) return launch_hsum_t<4>(p, s);
+  if (p.n_planes <= 8) return launch_hsum_t<8>(p, s);
+  return launch_hsum_t<16>(p, s);
+}
+
+cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
+  recheck_kernel<<<16, 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const FinalizeParams &p, int n_planes, cudaStream_t s) {
+  const int smem = kSortCap * (8 + 4);
+  cudaError_t e = cudaFuncSetAttribute(finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  finalize_kernel<<<n_planes, 1024, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace fdas

@@ -1,0 +1,241 @@
+/*
+ * fdas_gb300 -- C ABI of the GB300-native FDAS hot path.
+ *
+ * Each entry point replaces one method of the reference's host class
+ * `FDAS` (fdas/src/host/FDAS.h:36-187 in UOA-PARC-SKA/FDAS) and keeps its call
+ * sequence: template upload, threshold upload, input tiling, FT convolution,
+ * harmonic summing, candidate retrieval, with `launch` / `wait` enqueueing the
+ * whole pipeline asynchronously on one of two buffer sets (A/B).
+ *
+ * Differences from the reference, by design:
+ *  - errors are returned as `fdas_status` (never abort); a message is kept per
+ *    handle and returned by `fdas_last_error` (the reference logs and returns
+ *    `false`, FDAS.cpp:34-52);
+ *  - sizes (bins, templates, overlap, planes, candidate capacity) are runtime
+ *    configuration instead of the generated constants of gen_info.h;
+ *  - `FDAS_ALL_ACCELERATIONS` is supported by harmonic summing (the reference's
+ *    systolic detector rejects it, FDAS.cpp:447-450); template 0 is then
+ *    reported once;
+ *  - the candidate list is deterministic: every hit is kept (up to a
+ *    capacity), the 4096-entry reference-format list holds per plane the
+ *    strongest `candidates_per_plane_compat` hits in location order.
+ *
+ * A handle is single-threaded: calls on one handle must not run concurrently.
+ * Several handles may share a device.
+ */
+#ifndef FDAS_GB300_H
+#define FDAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fdas_handle fdas_handle;
+
+/* A complex single-precision value, layout-compatible with cl_float2 and
+ * std::complex<float>. */
+typedef struct {
+  float re;
+  float im;
+} fdas_complex;
+
+typedef enum {
+  FDAS_OK = 0,
+  FDAS_ERR_INVALID_ARG = 1,
+  FDAS_ERR_OUT_OF_MEMORY = 2,
+  FDAS_ERR_CUDA = 3,
+  FDAS_ERR_TIMEOUT = 4,
+  FDAS_ERR_UNSUPPORTED = 5,
+  FDAS_ERR_CAPACITY = 6,
+  FDAS_ERR_STATE = 7,
+  FDAS_ERR_NO_DEVICE = 8
+} fdas_status;
+
+/* FDAS::FOPPart (FDAS.h:38) */
+typedef enum {
+  FDAS_NEGATIVE_ACCELERATIONS = 0,
+  FDAS_POSITIVE_ACCELERATIONS = 1,
+  FDAS_ALL_ACCELERATIONS = 2
+} fdas_fop_part;
+
+/* FDAS::BufferSet (FDAS.h:39) */
+typedef enum { FDAS_SET_A = 0, FDAS_SET_B = 1 } fdas_buffer_set;
+
+/* FDAS::BufferMode (FDAS.h:40).  DDR bank placement on the FPGA board; on a
+ * GB300 all buffers live in the same HBM, so the modes are accepted and only
+ * recorded. */
+typedef enum { FDAS_MODE_PER_SET = 0, FDAS_MODE_PER_STAGE = 1, FDAS_MODE_CROSSED = 2 } fdas_buffer_mode;
+
+/* Layout of the array given to fdas_upload_templates. */
+typedef enum {
+  /* n_templates x 2048 spectra in the reference's "FFT order" with 4 parallel
+   * inputs (fdas_templates_85_350_ft_p4.npy, tmpl-gen.py:145-153) */
+  FDAS_TEMPLATES_FFT_P4 = 0,
+  /* n_templates x 2048 spectra in natural bin order */
+  FDAS_TEMPLATES_FFT_NATURAL = 1,
+  /* n_templates x max_template_len time-domain taps, left aligned and zero
+   * padded (fdas_templates_85_350.npy); spectra are computed on the device in
+   * FP64 and the taps are kept for the FP64 recheck */
+  FDAS_TEMPLATES_TIME_DOMAIN = 2
+} fdas_template_layout;
+
+typedef struct {
+  uint32_t n_frequency_bins;   /* N, the input size (FDAS::initialise_accelerator input_sz) */
+  uint32_t n_templates;        /* odd; 85 in the reference (gen_info.h:27) */
+  uint32_t max_template_len;   /* 421 in the reference (gen_info.h:28) */
+  uint32_t tile_overlap;       /* 0 = ceil((max_template_len - 1) / 4) * 4 (cl_codegen.py:99) */
+  uint32_t n_planes;           /* harmonic planes, 1..16 (8 in the reference) */
+  uint32_t candidate_capacity; /* hits kept per plane on the device; 0 = 8192 (max 8192) */
+  uint32_t candidates_per_plane_compat; /* entries per plane in the fixed list; 0 = 512 */
+  int32_t device;              /* CUDA device ordinal */
+  uint32_t buffer_mode;        /* fdas_buffer_mode */
+  uint32_t sync_pipeline;      /* FDAS::initialise_accelerator sync_pipeline */
+  uint32_t recheck;            /* 1 = FP64 recheck of near-threshold cells (default) */
+  float recheck_band;          /* relative band around each threshold; 0 = 1e-4 */
+} fdas_config;
+
+/* Fill `cfg` with the reference's defaults for `n_frequency_bins` bins. */
+void fdas_default_config(fdas_config *cfg, uint32_t n_frequency_bins);
+
+/* FDAS::FDAS + FDAS::initialise_accelerator (FDAS.h:42-49, FDAS.cpp:54-261).
+ * Allocates both buffer sets on `cfg->device`.  On failure *out is NULL and the
+ * message is available from fdas_last_error(NULL). */
+fdas_status fdas_initialise_accelerator(const fdas_config *cfg, fdas_handle **out);
+
+/* Releases all device resources of the handle. */
+void fdas_destroy(fdas_handle *h);
+
+/* Last error message of `h` (or of the last failed initialisation if h is NULL). */
+const char *fdas_last_error(const fdas_handle *h);
+
+/* FDAS::upload_templates (FDAS.h:51, FDAS.cpp:263-269).  `templates` is a host
+ * array of n_templates x 2048 complex values (FFT layouts) or n_templates x
+ * max_template_len taps (FDAS_TEMPLATES_TIME_DOMAIN).  Blocking. */
+fdas_status fdas_upload_templates(fdas_handle *h, const fdas_complex *templates, fdas_template_layout layout,
+                                  fdas_buffer_set ab);
+
+/* FDAS::upload_thresholds (FDAS.h:53, FDAS.cpp:271-280): n_planes floats,
+ * used when fdas_perform_harmonic_summing / fdas_launch get thresholds == NULL. */
+fdas_status fdas_upload_thresholds(fdas_handle *h, const float *thresholds, fdas_buffer_set ab);
+
+/* FDAS::perform_input_tiling (FDAS.h:55, FDAS.cpp:319-328): copy the N-bin
+ * spectrum to the device, build the overlap-save tiles and transform them.
+ * Blocking. */
+fdas_status fdas_perform_input_tiling(fdas_handle *h, const fdas_complex *input, fdas_buffer_set ab);
+
+/* FDAS::perform_ft_convolution (FDAS.h:57, FDAS.cpp:396-405): template
+ * multiply + inverse FFT + |.|^2 + overlap discard into the FOP rows of `which`.
+ * Blocking. */
+fdas_status fdas_perform_ft_convolution(fdas_handle *h, fdas_fop_part which, fdas_buffer_set ab);
+
+/* FDAS::perform_harmonic_summing (FDAS.h:59, FDAS.cpp:533-546).  Blocking. */
+fdas_status fdas_perform_harmonic_summing(fdas_handle *h, const float *thresholds, fdas_fop_part which,
+                                          fdas_buffer_set ab);
+
+/* FDAS::launch (FDAS.h:61, FDAS.cpp:548-583): enqueue tiling, FT convolution,
+ * harmonic summing and the candidate download into the caller's
+ * `detection_location` / `detection_power` (get_candidate_list_sz() entries
+ * each).  Returns without waiting; use fdas_wait. */
+fdas_status fdas_launch(fdas_handle *h, const fdas_complex *input, const float *thresholds,
+                        uint32_t *detection_location, float *detection_power, fdas_fop_part which,
+                        fdas_buffer_set ab);
+
+/* FDAS::wait (FDAS.h:63, FDAS.cpp:585-588): block until the last launch on
+ * `ab` has delivered its candidates.  Returns FDAS_ERR_STATE if that launch's
+ * harmonic summing is still held back by sync_pipeline (the reference would
+ * block forever there). */
+fdas_status fdas_wait(fdas_handle *h, fdas_buffer_set ab);
+
+/* FDAS::end_pipeline (FDAS.h:65, FDAS.cpp:590-594): release the held-back
+ * stage of the other set (sync_pipeline mode). */
+fdas_status fdas_end_pipeline(fdas_handle *h, fdas_buffer_set ab);
+
+/* FDAS::retrieve_tiles (FDAS.h:67, FDAS.cpp:596-599): n_tiles x 2048 tile
+ * spectra in the reference's p4 FFT order.  Blocking. */
+fdas_status fdas_retrieve_tiles(fdas_handle *h, fdas_complex *tiles, fdas_buffer_set ab);
+
+/* FDAS::retrieve_FOP (FDAS.h:69, FDAS.cpp:601-604): n_templates x N floats,
+ * row = template number + n_templates/2.  Blocking. */
+fdas_status fdas_retrieve_fop(fdas_handle *h, float *fop, fdas_buffer_set ab);
+
+/* FDAS::inject_FOP (FDAS.h:71, FDAS.cpp:628-632): replace the FOP of `ab`
+ * (the stage seam for harmonic-summing-only tests).  Harmonic summing of an
+ * injected FOP runs without the FP64 recheck, in plain FP32 like hsum.py. */
+fdas_status fdas_inject_fop(fdas_handle *h, const float *fop, fdas_buffer_set ab);
+
+/* FDAS::retrieve_candidates (FDAS.h:73, FDAS.cpp:619-626): the fixed-size
+ * list (get_candidate_list_sz() entries) of the last harmonic summing on `ab`:
+ * plane h occupies entries [h*P, (h+1)*P), P = candidates_per_plane_compat;
+ * unused entries hold location encode(1, 43, 0) and power -1.  Blocking. */
+fdas_status fdas_retrieve_candidates(fdas_handle *h, uint32_t *detection_location, float *detection_power,
+                                     fdas_buffer_set ab);
+
+/* Full candidate record (wide form; no 8-plane / 127-template / 2^22-bin limit). */
+typedef struct {
+  uint32_t harmonic;    /* 1..n_planes */
+  int32_t template_num; /* -n_templates/2 .. n_templates/2 */
+  uint32_t bin;         /* frequency bin */
+  float power;          /* harmonic-plane power HP_harmonic(template, bin) */
+} fdas_candidate;
+
+/* Every hit of the last harmonic summing on `ab`, sorted by (harmonic,
+ * template, bin) -- the order of hsum.py's list.  Writes min(total, capacity)
+ * records; *n_total gets the number of hits found, *n_dropped the hits lost to
+ * the device capacity (candidate_capacity per plane).  Blocking. */
+fdas_status fdas_retrieve_candidate_list(fdas_handle *h, fdas_candidate *out, uint32_t capacity,
+                                         uint32_t *n_total, uint32_t *n_dropped, fdas_buffer_set ab);
+
+/* FDAS::print_stats / print_events (FDAS.h:75-77, FDAS.cpp:643-686): write the
+ * stage timings of the last launch on `ab` to the log (stderr by default). */
+void fdas_print_stats(fdas_handle *h, fdas_buffer_set ab, int reset);
+void fdas_print_events(fdas_handle *h, fdas_buffer_set ab);
+
+/* Redirect the handle's log lines ("[INFO] ...", "@@@,...") to a callback. */
+typedef void (*fdas_log_fn)(const char *line, void *user);
+void fdas_set_log(fdas_handle *h, fdas_log_fn fn, void *user);
+
+/* Stage times of the last completed launch on `ab`, in milliseconds:
+ * [0] input copy, [1] tiling, [2] FT convolution, [3] harmonic summing,
+ * [4] candidate download, [5] total. */
+fdas_status fdas_get_stage_times(fdas_handle *h, fdas_buffer_set ab, float *ms6);
+
+/* FDAS::get_*_sz (FDAS.h:79-89, FDAS.cpp:688-711) -- element counts. */
+uint32_t fdas_get_input_sz(const fdas_handle *h);
+uint32_t fdas_get_tiles_sz(const fdas_handle *h);
+uint32_t fdas_get_templates_sz(const fdas_handle *h);
+uint32_t fdas_get_thresholds_sz(const fdas_handle *h);
+uint32_t fdas_get_fop_sz(const fdas_handle *h);
+uint32_t fdas_get_candidate_list_sz(const fdas_handle *h);
+
+/* Pinned host memory for the copy-in / copy-out buffers (replaces
+ * AlignedBuffer, fdas/src/host/AlignedBuffer.h:26-52). */
+fdas_status fdas_host_alloc(void **ptr, size_t bytes);
+void fdas_host_free(void *ptr);
+fdas_status fdas_host_register(void *ptr, size_t bytes);
+fdas_status fdas_host_unregister(void *ptr);
+
+/* ------------------------------------------------------------------------
+ * Device-resident entry points (no counterpart in the reference).  They let a
+ * caller whose spectrum already sits in device memory run the same pipeline
+ * without the host copy: `d_input` is a device pointer to N complex values.
+ * The work is enqueued on the set's stream; candidates stay on the device
+ * until fdas_retrieve_candidates / fdas_retrieve_candidate_list.
+ * ---------------------------------------------------------------------- */
+fdas_status fdas_enqueue_search_device(fdas_handle *h, const fdas_complex *d_input, const float *thresholds,
+                                       fdas_fop_part which, fdas_buffer_set ab);
+/* Block until all work enqueued on `ab` is done. */
+fdas_status fdas_synchronize(fdas_handle *h, fdas_buffer_set ab);
+/* The CUDA stream (cudaStream_t) of buffer set `ab`. */
+void *fdas_get_stream(fdas_handle *h, fdas_buffer_set ab);
+
+/* Library version string. */
+const char *fdas_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDAS_GB300_H */

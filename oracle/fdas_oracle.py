@@ -298,3 +298,45 @@ def search(ft, templates, thresholds, n_planes=8, part='all', dtype=np.float64):
     hps = harmonic_planes(plane, n_planes, dtype=dtype)
     rows = part_rows(part, plane.shape[0])
     return plane, hps, detections(hps, thresholds, rows)
+
+
+def detections_streaming(fop_plane, thresholds, n_planes=8, part='all', dtype=np.float64):
+    """Candidates of a whole search without materialising all harmonic planes.
+
+    Same semantics as ``harmonic_planes`` + ``detections`` (sequential
+    accumulation HP_k = HP_{k-1} + FOP[trunc(t/k)][f//k] in ``dtype``), one
+    plane at a time, for full-size (2^21-bin) checks.
+    Returns (location, power, plane, row, bin) sorted by location.
+    """
+    f = np.asarray(fop_plane).astype(dtype, copy=False)
+    n_tmpl, n_freq = f.shape
+    rows = part_rows(part, n_tmpl)
+    hp = f[rows].copy()
+    freqs = np.arange(n_freq)
+    out = ([], [], [], [], [])
+    for h in range(n_planes):
+        k = h + 1
+        if k > 1:
+            hp += f[subharmonic_row(rows, k, n_tmpl)][:, freqs // k]
+        ri, fi = np.nonzero(hp > np.asarray(thresholds[h], dtype=dtype))
+        out[0].append(encode_location(k, rows[ri] - n_tmpl // 2, fi))
+        out[1].append(hp[ri, fi])
+        out[2].append(np.full(ri.size, h, dtype=np.int64))
+        out[3].append(rows[ri])
+        out[4].append(fi)
+    loc = np.concatenate(out[0])
+    order = np.argsort(loc, kind='stable')
+    return tuple(np.concatenate(o)[order] for o in out)
+
+
+def hp_cells(fop_plane, plane, rows, bins, dtype=np.float64):
+    """HP_{plane+1} at individual cells (sequential accumulation)."""
+    f = np.asarray(fop_plane)
+    n_tmpl = f.shape[0]
+    out = np.zeros(len(rows), dtype=dtype)
+    for i, (p, r, b) in enumerate(zip(plane, rows, bins)):
+        acc = dtype(0)
+        for k in range(1, int(p) + 2):
+            acc = dtype(acc + dtype(f[subharmonic_row(int(r), k, n_tmpl), int(b) // k]))
+        out[i] = acc
+    return out

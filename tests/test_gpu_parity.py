@@ -1,0 +1,312 @@
+"""GPU parity tests: the CUDA path through the C ABI against the oracle.
+
+Checks follow the reference's gtest (fdas/src/host/main_gtest.cpp:173-228) and
+add the stricter FP64 criteria: FOP within 1e-5 of the plane's mean power of
+the FP64 oracle, candidate sets identical to the FP64 oracle's (near-threshold
+cells are decided by the FP64 recheck), and harmonic summing of an injected FOP
+bit-exact with hsum.py.
+"""
+import io
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from gpu_util import make_pipeline, candidates_as_arrays, validate_harmonic_summing
+from fdas_gb300.fdas import FDAS
+from fdas_gb300.templates import template_bank
+from fdas_gb300 import synth
+from oracle import fdas_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FOP_REL_TOL = 1e-5  # |FOP_gpu - FOP_fp64| <= 1e-5 * mean power of the plane
+
+
+@pytest.fixture(scope="module")
+def bank64():
+    return template_bank()
+
+
+@pytest.fixture(scope="module")
+def bank_p4(bank64):
+    return O.to_p4(np.fft.fft(bank64.astype(np.complex128), 2048, axis=1)).astype(np.complex64)
+
+
+def run_ftc(g_input, bank, layout, part=FDAS.AllAccelerations):
+    n = g_input.size
+    p = make_pipeline(n, log=io.StringIO())
+    assert p.upload_templates(bank, FDAS.A, layout=layout), p.last_error
+    assert p.perform_input_tiling(g_input, FDAS.A), p.last_error
+    assert p.perform_ft_convolution(part, FDAS.A), p.last_error
+    tiles = np.zeros(p.get_tiles_sz(), dtype=np.complex64)
+    assert p.retrieve_tiles(tiles, FDAS.A)
+    fop = np.zeros(p.get_fop_sz(), dtype=np.float32)
+    assert p.retrieve_FOP(fop, FDAS.A)
+    return p, tiles.reshape(-1, 2048), fop.reshape(85, n)
+
+
+@pytest.mark.parametrize("name", ["n1000", "n4096", "n32768"])
+def test_tiles_match_reference(name, bank_p4):
+    g = load_golden(name)
+    _, tiles, _ = run_ftc(g["input"], bank_p4, FDAS.TemplatesFFTP4)
+    assert tiles.shape[0] == int(g["n_tiles"])
+    # main_gtest.cpp:173-181: |d re|, |d im| < 1e-5 against input_tiled_p4_ref
+    d = tiles[g["tile_idx"]] - g["tiles_p4_ref"]
+    assert np.abs(d.real).max() < 1e-5 and np.abs(d.imag).max() < 1e-5
+    # and against the FP64 tiles, relative to the tile rms
+    ref = O.to_p4(O.tiles(g["input"]))
+    rms = np.sqrt(np.mean(np.abs(ref) ** 2))
+    assert np.abs(tiles - ref).max() < 1e-5 * rms
+
+
+@pytest.mark.parametrize("name", ["n1000", "n4096", "n32768"])
+@pytest.mark.parametrize("layout", ["p4", "time"])
+def test_fop_vs_fp64_oracle(name, layout, bank64, bank_p4):
+    g = load_golden(name)
+    bank = bank_p4 if layout == "p4" else bank64
+    lay = FDAS.TemplatesFFTP4 if layout == "p4" else FDAS.TemplatesTimeDomain
+    _, _, fop = run_ftc(g["input"], bank, lay)
+    ref = O.fop(g["input"], bank64)
+    mean = ref.mean(axis=1, keepdims=True)
+    err = np.abs(fop - ref) / mean
+    assert err.max() <= FOP_REL_TOL, err.max()
+    # main_gtest.cpp:183-190 absolute check against the reference's own FOP
+    assert np.abs(fop[g["fop_rows"]] - g["fop_ref"]).max() < 1e-5
+
+
+@pytest.mark.parametrize("part", [FDAS.NegativeAccelerations, FDAS.PositiveAccelerations])
+def test_fop_part_rows_only(part, bank_p4):
+    g = load_golden("n4096")
+    _, _, fop = run_ftc(g["input"], bank_p4, FDAS.TemplatesFFTP4, part=part)
+    rows = np.arange(0, 43) if part == FDAS.NegativeAccelerations else np.arange(42, 85)
+    other = np.setdiff1d(np.arange(85), rows)
+    ref = O.fop(g["input"], template_bank(), rows=rows)
+    assert np.abs(fop[rows] - ref).max() <= FOP_REL_TOL * ref.mean()
+    assert np.all(fop[other] == 0)  # untouched rows of a fresh buffer set
+
+
+@pytest.mark.parametrize("name", ["n1000", "n4096"])
+@pytest.mark.parametrize("thr_key", ["", "_chi2"])
+def test_hsum_injected_fop_bit_exact(name, thr_key):
+    """inject_FOP(fop_ref) -> harmonic summing: identical to hsum.py's list."""
+    g = load_golden(name)
+    n = g["input"].size
+    p = make_pipeline(n, log=io.StringIO())
+    thr = g["thresholds" + thr_key]
+    assert p.inject_FOP(g["fop_ref"], FDAS.A)
+    assert p.perform_harmonic_summing(thr, FDAS.AllAccelerations, FDAS.A), p.last_error
+    rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
+    assert dropped == 0
+    loc, pwr = candidates_as_arrays(rec)
+    assert np.array_equal(loc, g["det_loc_ref" + thr_key])
+    assert np.array_equal(pwr, g["det_pwr_ref" + thr_key])
+
+
+@pytest.mark.parametrize("part", [FDAS.NegativeAccelerations, FDAS.PositiveAccelerations])
+def test_hsum_injected_half_gtest_check(part):
+    """The reference's Harmonic_Summing test (main_gtest.cpp:261-283)."""
+    g = load_golden("n4096")
+    p = make_pipeline(4096, log=io.StringIO())
+    assert p.inject_FOP(g["fop_ref"], FDAS.A)
+    assert p.perform_harmonic_summing(g["thresholds"], part, FDAS.A)
+    n = p.get_candidate_list_sz()
+    assert n == 4096
+    loc = np.zeros(n, dtype=np.uint32)
+    pwr = np.zeros(n, dtype=np.float32)
+    assert p.retrieve_candidates(loc, pwr, FDAS.A)
+    validate_harmonic_summing(loc, pwr, g["det_loc_ref"], g["det_pwr_ref"])
+    # every hit of the half is present (the list holds up to 512 per plane)
+    h, t, f = O.decode_location(g["det_loc_ref"])
+    want = (t <= 0) if part == FDAS.NegativeAccelerations else (t >= 0)
+    got = set(loc[loc != O.INVALID_LOCATION].tolist())
+    assert got == set(g["det_loc_ref"][want].tolist())
+
+
+@pytest.mark.parametrize("name,thr_key", [("n4096", ""), ("n4096", "_chi2"), ("n32768", ""),
+                                          ("n32768", "_chi2")])
+@pytest.mark.parametrize("layout", ["time", "p4"])
+def test_search_candidates_equal_fp64_oracle(name, thr_key, layout, bank64, bank_p4):
+    """Full search (launch/wait): candidate set identical to the FP64 oracle's."""
+    g = load_golden(name)
+    n = g["input"].size
+    thr = g["thresholds" + thr_key]
+    p = make_pipeline(n, log=io.StringIO())
+    bank = bank64 if layout == "time" else bank_p4
+    assert p.upload_templates(bank, FDAS.A)
+    loc = np.zeros(p.get_candidate_list_sz(), dtype=np.uint32)
+    pwr = np.zeros_like(loc, dtype=np.float32)
+    assert p.launch(g["input"], thr, loc, pwr, FDAS.AllAccelerations, FDAS.A), p.last_error
+    assert p.wait(FDAS.A), p.last_error
+    rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
+    assert dropped == 0
+    gl, gp = candidates_as_arrays(rec)
+    fop64 = O.fop(g["input"], bank64)
+    ol, op, *_ = O.detections(O.harmonic_planes(fop64, 8, dtype=np.float64), thr)
+    if layout == "time":
+        assert np.array_equal(gl, ol)
+    else:
+        # FP32 template spectra: the recheck's filter differs from the
+        # time-domain taps by ~1e-7 relative; allow cells that close
+        diff = set(gl.tolist()) ^ set(ol.tolist())
+        hps = O.harmonic_planes(fop64, 8, dtype=np.float64)
+        for d in diff:
+            hh, tt, ff = O.decode_location(d)
+            assert abs(hps[hh - 1][tt + 42][ff] - thr[hh - 1]) <= 1e-6 * thr[hh - 1]
+    common = np.isin(gl, ol)
+    ref_p = dict(zip(ol.tolist(), op.tolist()))
+    rp = np.array([ref_p[x] for x in gl[common].tolist()])
+    assert np.all(np.abs(gp[common] - rp) <= 8 * FOP_REL_TOL * fop64.mean() + 1e-6 * np.abs(rp))
+    # the fixed-size list holds the strongest per plane, as the oracle's rule says
+    cl, cp = O.compat_list(ol, op.astype(np.float32), (ol >> 29).astype(np.int64))
+    if layout == "time":
+        assert np.array_equal(loc, cl)
+
+
+def test_candidate_capacity_and_compat_overflow():
+    """More hits than the fixed list holds: strongest 512 per plane, in location order."""
+    g = load_golden("n4096")
+    thr = np.full(8, 0.0, dtype=np.float32)
+    thr[:] = np.quantile(g["fop_ref"], 0.99)  # thousands of hits per plane
+    p = make_pipeline(4096, log=io.StringIO())
+    assert p.inject_FOP(g["fop_ref"], FDAS.A)
+    assert p.perform_harmonic_summing(thr, FDAS.AllAccelerations, FDAS.A)
+    rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
+    hps = O.harmonic_planes(g["fop_ref"].astype(np.float32), 8, dtype=np.float32)
+    ol, op, opl, *_ = O.detections(hps, thr)
+    assert total == ol.size
+    if dropped == 0:
+        loc, pwr = candidates_as_arrays(rec)
+        assert np.array_equal(loc, ol) and np.array_equal(pwr, op)
+    cloc = np.zeros(4096, dtype=np.uint32)
+    cpwr = np.zeros(4096, dtype=np.float32)
+    assert p.retrieve_candidates(cloc, cpwr, FDAS.A)
+    el, ep = O.compat_list(ol, op, opl)
+    if dropped == 0:
+        assert np.array_equal(cloc, el) and np.array_equal(cpwr, ep)
+
+
+def _drive(sync_pipeline, n_runs=4):
+    """main_gtest.cpp drive_serially / drive_pipelined with the p4 bank."""
+    g = load_golden("n4096")
+    bank_p4 = O.to_p4(np.fft.fft(template_bank().astype(np.complex128), 2048, axis=1)).astype(np.complex64)
+    p = make_pipeline(4096, log=io.StringIO(), sync_pipeline=sync_pipeline)
+    assert p.upload_templates(bank_p4, FDAS.A)
+    assert p.upload_templates(bank_p4, FDAS.B)
+    n = p.get_candidate_list_sz()
+    loc = {ab: np.zeros(n, dtype=np.uint32) for ab in (FDAS.A, FDAS.B)}
+    pwr = {ab: np.zeros(n, dtype=np.float32) for ab in (FDAS.A, FDAS.B)}
+    thr = g["thresholds"]
+    if not sync_pipeline:
+        for i in range(n_runs):
+            which = FDAS.PositiveAccelerations if i % 2 == 0 else FDAS.NegativeAccelerations
+            assert p.launch(g["input"], thr, loc[FDAS.A], pwr[FDAS.A], which, FDAS.A)
+            assert p.wait(FDAS.A), p.last_error
+            p.print_stats(FDAS.A, i == 0)
+            p.print_events(FDAS.A)
+        sets = [FDAS.A]
+    else:
+        which = {FDAS.A: FDAS.PositiveAccelerations, FDAS.B: FDAS.NegativeAccelerations}
+        for i in range(n_runs + 1):
+            ab, prev = (FDAS.A, FDAS.B) if i % 2 == 0 else (FDAS.B, FDAS.A)
+            if i < n_runs:
+                assert p.launch(g["input"], thr, loc[ab], pwr[ab], which[ab], ab), p.last_error
+            else:
+                assert p.end_pipeline(ab)
+            if i > 0:
+                assert p.wait(prev), p.last_error
+                p.print_stats(prev, i - 1 == 0)
+                p.print_events(prev)
+        sets = [FDAS.A, FDAS.B]
+    for ab in sets:
+        validate_harmonic_summing(loc[ab], pwr[ab], g["det_loc_ref"], g["det_pwr_ref"], tol=1e-5 * 8)
+    return p
+
+
+def test_drive_serially():
+    _drive(False)
+
+
+def test_drive_pipelined():
+    p = _drive(True)
+    # a set whose harmonic summing is held back cannot be waited on
+    g = load_golden("n4096")
+    loc = np.zeros(p.get_candidate_list_sz(), dtype=np.uint32)
+    pwr = np.zeros_like(loc, dtype=np.float32)
+    assert p.launch(g["input"], g["thresholds"], loc, pwr, FDAS.AllAccelerations, FDAS.A)
+    assert not p.wait(FDAS.A)
+    assert p.end_pipeline(FDAS.B)
+    assert p.wait(FDAS.A)
+
+
+@pytest.mark.parametrize("n_bins", [1, 7, 1627, 1628, 1629, 3001, 2 * 1628 + 1])
+def test_edge_sizes(n_bins, bank64):
+    """Ragged sizes: a single bin, a partial first tile, exact tile multiples."""
+    rng = np.random.default_rng(n_bins)
+    x = (rng.standard_normal(n_bins) + 1j * rng.standard_normal(n_bins)).astype(np.complex64) / np.sqrt(2)
+    p = make_pipeline(n_bins, log=io.StringIO())
+    assert p.upload_templates(bank64, FDAS.A)
+    thr = O.chi2_thresholds(1e-3)
+    loc = np.zeros(p.get_candidate_list_sz(), dtype=np.uint32)
+    pwr = np.zeros_like(loc, dtype=np.float32)
+    assert p.launch(x, thr, loc, pwr, FDAS.AllAccelerations, FDAS.A)
+    assert p.wait(FDAS.A)
+    fop = np.zeros(p.get_fop_sz(), dtype=np.float32)
+    assert p.retrieve_FOP(fop, FDAS.A)
+    ref = O.fop(x, bank64)
+    assert np.abs(fop.reshape(85, n_bins) - ref).max() <= FOP_REL_TOL * max(ref.mean(), 1e-30)
+    rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
+    gl, _ = candidates_as_arrays(rec)
+    ol, *_ = O.detections(O.harmonic_planes(ref, 8, dtype=np.float64), thr)
+    assert np.array_equal(gl, ol)
+
+
+def test_invalid_arguments_fail_loudly():
+    p = FDAS(io.StringIO())
+    assert not p.initialise_accelerator(0)
+    assert not p.initialise_accelerator(4096, n_templates=84)
+    assert not p.initialise_accelerator(4096, n_planes=17)
+    assert not p.initialise_accelerator(4096, tile_overlap=100)  # < 421 - 1
+    p = make_pipeline(4096, log=io.StringIO())
+    # no templates uploaded yet
+    assert p.perform_input_tiling(np.zeros(4096, np.complex64), FDAS.A)
+    assert not p.perform_ft_convolution(FDAS.AllAccelerations, FDAS.A)
+    assert "templates" in p.last_error
+    assert not p.wait(FDAS.B)  # nothing launched
+    assert not p.launch(np.zeros(4096, np.complex64), None, np.zeros(4096, np.uint32), np.zeros(4096, np.float32),
+                        FDAS.AllAccelerations, FDAS.A)  # no thresholds given or uploaded
+
+
+def test_full_size_properties(bank64):
+    """2^21 bins: FOP rows against the FP64 oracle and the candidate set vs FP64."""
+    samples, sig = synth.full_case()
+    x, scale = synth.spectrum(samples)
+    n = x.size
+    assert n == 1 << 21
+    thr = O.chi2_thresholds(1e-6)
+    p = make_pipeline(n, log=io.StringIO())
+    assert p.upload_templates(bank64, FDAS.A)
+    loc = np.zeros(p.get_candidate_list_sz(), dtype=np.uint32)
+    pwr = np.zeros_like(loc, dtype=np.float32)
+    assert p.launch(x, thr, loc, pwr, FDAS.AllAccelerations, FDAS.A)
+    assert p.wait(FDAS.A)
+    fop = np.zeros(p.get_fop_sz(), dtype=np.float32)
+    assert p.retrieve_FOP(fop, FDAS.A)
+    fop = fop.reshape(85, n)
+    fop64 = O.fop(x, bank64)
+    mean = fop64.mean(axis=1, keepdims=True)
+    # strong injected signals make FP32 rounding of the largest cells exceed
+    # 1e-5 of the mean; the bound used is 1e-5 of the mean plus 2^-20 relative
+    err = np.abs(fop - fop64)
+    assert np.all(err <= FOP_REL_TOL * mean + 2.0 ** -20 * np.abs(fop64))
+    noise_rows = err / mean
+    assert np.median(noise_rows.max(axis=1)) <= FOP_REL_TOL
+    rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
+    assert dropped == 0
+    gl, gp = candidates_as_arrays(rec)
+    ol, op, *_ = O.detections_streaming(fop64, thr)
+    assert np.array_equal(gl, ol)
+    # every injected signal is detected near its starting bin
+    h, t, f = O.decode_location(gl)
+    for s in sig:
+        assert (np.abs(f - s["r0"]) < 1000).any(), s
