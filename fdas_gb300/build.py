@@ -68,7 +68,30 @@ def build(verbose=False, force=False, ptxas_verbose=False):
         if r.returncode != 0:
             sys.stderr.write(r.stderr)
             raise RuntimeError("link failed")
+    build_driver(force=force)
     return LIB
+
+
+DRIVER_SRC = ROOT / "tests" / "cpp" / "fdas_drive.cpp"
+DRIVER = BUILD / "fdas_drive"
+
+
+def build_driver(force=False):
+    """C++ driver over include/FDAS.hpp (the reference-style host class), linked
+    against the library; used by the GPU tests."""
+    if not DRIVER_SRC.exists():
+        return None
+    if not force and DRIVER.exists() and DRIVER.stat().st_mtime > max(
+            DRIVER_SRC.stat().st_mtime, LIB.stat().st_mtime, (ROOT / "include" / "FDAS.hpp").stat().st_mtime):
+        return DRIVER
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", f"-I{ROOT / 'include'}", str(DRIVER_SRC), f"-L{PKG}", "-lfdas_gb300",
+           f"-Wl,-rpath,{PKG}", "-o", str(DRIVER)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stderr)
+        raise RuntimeError("C++ driver build failed")
+    return DRIVER
 
 
 if __name__ == "__main__":

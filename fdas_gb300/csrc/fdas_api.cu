@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <numeric>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -24,10 +25,16 @@ namespace {
 
 thread_local std::string g_init_error;
 
+// device control words of a buffer set (zeroed before every harmonic summing)
 constexpr int kCtrlStatus = 0;
 constexpr int kCtrlRecheckCount = 1;
-constexpr int kCtrlCount = 2;  // + plane
-constexpr int kCtrlWords = 2 + kMaxPlanes;
+constexpr int kCtrlTotal = 2;                       // records appended
+constexpr int kCtrlCount = 3;                       // + plane: hits per plane
+constexpr int kCtrlSelCount = kCtrlCount + kMaxPlanes;
+constexpr int kCtrlSelLo = kCtrlSelCount + kMaxPlanes;
+constexpr int kCtrlWords = kCtrlSelLo + kMaxPlanes;
+constexpr uint32_t kDefaultCapacity = 1u << 22;     // candidate records per buffer set
+constexpr uint32_t kMaxCapacity = 1u << 27;
 constexpr int kRecheckCap = 65536;
 constexpr int kNumEvents = 6;  // start, input, tiling, ftc, hsum, done
 
@@ -45,6 +52,9 @@ struct BufferSet {
   unsigned *d_ctrl = nullptr;
   unsigned *h_ctrl = nullptr;  // pinned mirror of d_ctrl
   uint4 *d_rc = nullptr;
+  unsigned *d_hist = nullptr;
+  unsigned long long *d_sel_key = nullptr;
+  float *d_sel_pwr = nullptr;
   uint32_t *d_cloc = nullptr;
   float *d_cpwr = nullptr;
   cudaEvent_t ev[kNumEvents] = {};
@@ -252,6 +262,7 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   p.stage_bytes = bytes;
   p.cand_key = S.d_key;
   p.cand_pwr = S.d_pwr;
+  p.cand_total = S.d_ctrl + kCtrlTotal;
   p.cand_count = S.d_ctrl + kCtrlCount;
   p.cand_cap = h->cap;
   p.rc_list = S.d_rc;
@@ -276,21 +287,30 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
     r.rc_cap = kRecheckCap;
     r.cand_key = S.d_key;
     r.cand_pwr = S.d_pwr;
+    r.cand_total = S.d_ctrl + kCtrlTotal;
     r.cand_count = S.d_ctrl + kCtrlCount;
     r.cand_cap = h->cap;
     r.status = p.status;
     CK(h, launch_recheck(r, S.stream));
   }
-  FinalizeParams f{};
+  SelectParams f{};
   f.cand_key = S.d_key;
   f.cand_pwr = S.d_pwr;
+  f.cand_total = S.d_ctrl + kCtrlTotal;
   f.cand_count = S.d_ctrl + kCtrlCount;
   f.cand_cap = h->cap;
+  f.n_planes = P;
   f.per_plane = h->per_plane;
+  f.hist = S.d_hist;
+  f.sel_lo = S.d_ctrl + kCtrlSelLo;
+  f.sel_key = S.d_sel_key;
+  f.sel_pwr = S.d_sel_pwr;
+  f.sel_count = S.d_ctrl + kCtrlSelCount;
   f.compat_loc = S.d_cloc;
   f.compat_pwr = S.d_cpwr;
-  f.invalid_location = (0u << 29) | ((uint32_t)((h->H + 1 + h->H) & 0x7f) << 22);  // encode(1, H+1, 0)
-  CK(h, launch_finalize(f, P, S.stream));
+  f.invalid_location = (uint32_t)((h->H + 1 + h->H) & 0x7f) << 22;  // encode(1, H+1, 0), gen_info.h:69
+  f.status = p.status;
+  CK(h, launch_select(f, S.stream));
   CK(h, cudaMemcpyAsync(S.h_ctrl, S.d_ctrl, sizeof(unsigned) * kCtrlWords, cudaMemcpyDeviceToHost, S.stream));
   CK(h, cudaEventRecord(S.ev[4], S.stream));
   S.ctrl_valid = true;
@@ -345,6 +365,9 @@ void free_set(BufferSet &S) {
   cudaFree(S.d_pwr);
   cudaFree(S.d_ctrl);
   cudaFree(S.d_rc);
+  cudaFree(S.d_hist);
+  cudaFree(S.d_sel_key);
+  cudaFree(S.d_sel_pwr);
   cudaFree(S.d_cloc);
   cudaFree(S.d_cpwr);
   if (S.h_ctrl) cudaFreeHost(S.h_ctrl);
@@ -396,10 +419,10 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
   if (O + 1 < cfg.max_template_len)
     return fail(nullptr, FDAS_ERR_INVALID_ARG, "tile_overlap must be >= max_template_len - 1 (overlap-save)");
   if (O >= (uint32_t)kTile) return fail(nullptr, FDAS_ERR_INVALID_ARG, "tile_overlap must be < 2048");
-  uint32_t cap = cfg.candidate_capacity ? cfg.candidate_capacity : (uint32_t)kSortCap;
-  if (cap > (uint32_t)kSortCap) return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidate_capacity must be <= 8192");
+  uint32_t cap = cfg.candidate_capacity ? cfg.candidate_capacity : kDefaultCapacity;
+  if (cap > kMaxCapacity) return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidate_capacity must be <= 2^27");
   uint32_t pc = cfg.candidates_per_plane_compat ? cfg.candidates_per_plane_compat : 512u;
-  if (pc > cap) return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidates_per_plane_compat must be <= capacity");
+  if (pc > (uint32_t)kSortCap) return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidates_per_plane_compat must be <= 8192");
 
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -470,10 +493,13 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
         {(void **)&S.d_taps, sizeof(double2) * (size_t)h->T * h->tap_pitch},
         {(void **)&S.d_taplen, sizeof(int) * (size_t)h->T},
         {(void **)&S.d_fop, sizeof(float) * fop_floats},
-        {(void **)&S.d_key, sizeof(unsigned long long) * (size_t)h->P * h->cap},
-        {(void **)&S.d_pwr, sizeof(float) * (size_t)h->P * h->cap},
+        {(void **)&S.d_key, sizeof(unsigned long long) * (size_t)h->cap},
+        {(void **)&S.d_pwr, sizeof(float) * (size_t)h->cap},
         {(void **)&S.d_ctrl, sizeof(unsigned) * kCtrlWords},
         {(void **)&S.d_rc, sizeof(uint4) * kRecheckCap},
+        {(void **)&S.d_hist, sizeof(unsigned) * (size_t)h->P * kSelBuckets},
+        {(void **)&S.d_sel_key, sizeof(unsigned long long) * (size_t)h->P * kSortCap},
+        {(void **)&S.d_sel_pwr, sizeof(float) * (size_t)h->P * kSortCap},
         {(void **)&S.d_cloc, sizeof(uint32_t) * (size_t)h->P * h->per_plane},
         {(void **)&S.d_cpwr, sizeof(float) * (size_t)h->P * h->per_plane},
     };
@@ -486,6 +512,7 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
       }
     }
     if ((e = cudaMemset(S.d_fop, 0, sizeof(float) * fop_floats)) != cudaSuccess ||
+        (e = cudaMemset(S.d_hist, 0, sizeof(unsigned) * (size_t)h->P * kSelBuckets)) != cudaSuccess ||
         (e = cudaMemset(S.d_ctrl, 0, sizeof(unsigned) * kCtrlWords)) != cudaSuccess ||
         (e = cudaHostAlloc((void **)&S.h_ctrl, sizeof(unsigned) * kCtrlWords, cudaHostAllocDefault)) !=
             cudaSuccess ||
@@ -774,30 +801,30 @@ fdas_status fdas_retrieve_candidate_list(fdas_handle *h, fdas_candidate *out, ui
   BufferSet &S = h->set[ab];
   unsigned ctrl[kCtrlWords];
   CK(h, cudaMemcpy(ctrl, S.d_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
-  uint32_t total = 0, dropped = 0, written = 0;
-  std::vector<unsigned long long> keys;
-  std::vector<float> pwrs;
-  for (int pl = 0; pl < h->P; ++pl) {
-    const unsigned cnt = ctrl[kCtrlCount + pl];
-    const unsigned kept = std::min(cnt, (unsigned)h->cap);
-    total += cnt;
-    dropped += cnt - kept;
-    if (kept == 0 || written >= capacity) continue;
-    keys.resize(kept);
-    pwrs.resize(kept);
-    CK(h, cudaMemcpy(keys.data(), S.d_key + (size_t)pl * h->cap, sizeof(unsigned long long) * kept,
-                     cudaMemcpyDeviceToHost));
-    CK(h, cudaMemcpy(pwrs.data(), S.d_pwr + (size_t)pl * h->cap, sizeof(float) * kept, cudaMemcpyDeviceToHost));
-    for (unsigned i = 0; i < kept && written < capacity; ++i) {
-      fdas_candidate &c = out[written++];
-      c.harmonic = (uint32_t)pl + 1;
-      c.template_num = (int32_t)(keys[i] >> 32) - h->H;
-      c.bin = (uint32_t)(keys[i] & 0xffffffffu);
-      c.power = pwrs[i];
-    }
+  uint32_t total = 0;
+  for (int pl = 0; pl < h->P; ++pl) total += ctrl[kCtrlCount + pl];
+  const uint32_t stored = std::min(ctrl[kCtrlTotal], (unsigned)h->cap);
+  std::vector<unsigned long long> keys(stored);
+  std::vector<float> pwrs(stored);
+  if (stored) {
+    CK(h, cudaMemcpy(keys.data(), S.d_key, sizeof(unsigned long long) * stored, cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpy(pwrs.data(), S.d_pwr, sizeof(float) * stored, cudaMemcpyDeviceToHost));
+  }
+  // (harmonic, template, bin) order, as hsum.py lists its detections
+  std::vector<uint32_t> idx(stored);
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return keys[a] < keys[b]; });
+  const uint32_t n = std::min(stored, capacity);
+  for (uint32_t i = 0; i < n; ++i) {
+    const unsigned long long k = keys[idx[i]];
+    fdas_candidate &c = out[i];
+    c.harmonic = (uint32_t)(k >> 48) + 1;
+    c.template_num = (int32_t)((k >> 32) & 0xffffu) - h->H;
+    c.bin = (uint32_t)(k & 0xffffffffu);
+    c.power = pwrs[idx[i]];
   }
   if (n_total) *n_total = total;
-  if (n_dropped) *n_dropped = dropped;
+  if (n_dropped) *n_dropped = total - stored;
   return FDAS_OK;
 }
 

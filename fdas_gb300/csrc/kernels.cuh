@@ -10,11 +10,21 @@ constexpr int kTile = 2048;          // FFT / tile size (gen_info.h:33, 42)
 constexpr int kMaxPlanes = 16;       // harmonic planes supported by the kernels
 constexpr int kHsBins = 256;         // bins per harmonic-summing CTA
 constexpr int kHsThreads = 256;
-constexpr int kSortCap = 8192;       // per-plane candidate capacity (one-CTA sort)
+constexpr int kSortCap = 8192;       // records one CTA sorts in shared memory
+constexpr int kEmitBuf = 1024;       // candidate records staged per harmonic-summing CTA
+constexpr int kSelBuckets = 65536;   // power buckets of the top-K selection (top 16 key bits)
 
 // device status bits (per buffer set)
 constexpr int kStatusHsumTimeout = 1;
 constexpr int kStatusRecheckOverflow = 2;
+constexpr int kStatusCandidateOverflow = 4;
+constexpr int kStatusSelectionOverflow = 8;
+
+// Candidate record key: plane << 48 | row << 32 | bin.  Ascending key order is
+// (harmonic, template, bin) -- the order of hsum.py's list.
+__host__ __device__ inline unsigned long long cand_key(int plane, int row, int bin) {
+  return ((unsigned long long)(unsigned)plane << 48) | ((unsigned long long)(unsigned)row << 32) | (unsigned)bin;
+}
 
 // ---- (a) overlap-save tiling + forward FFT (tile_input.cl.mako, fft_4p.cl)
 struct TileParams {
@@ -60,9 +70,10 @@ struct HsumParams {
   int srows[kMaxPlanes + 1];// rows staged for plane j (= half / j + 1)
   unsigned stage_bytes;   // total bytes moved by the bulk copies
   int smem_floats;        // staging floats (after the 16-byte barrier slot)
-  unsigned long long *cand_key;  // [plane][cap] : (row << 32) | bin
-  float *cand_pwr;               // [plane][cap]
-  unsigned *cand_count;          // [plane]
+  unsigned long long *cand_key;  // [cap] records, any order
+  float *cand_pwr;               // [cap]
+  unsigned *cand_total;          // records appended (may exceed cap)
+  unsigned *cand_count;          // [plane] hits per plane
   int cand_cap;
   uint4 *rc_list;         // recheck entries (plane, row, bin, 0)
   unsigned *rc_count;
@@ -85,21 +96,30 @@ struct RecheckParams {
   int rc_cap;
   unsigned long long *cand_key;
   float *cand_pwr;
+  unsigned *cand_total;
   unsigned *cand_count;
   int cand_cap;
   int *status;
 };
 
-// ---- sort + fixed-size list
-struct FinalizeParams {
-  unsigned long long *cand_key;
-  float *cand_pwr;
-  const unsigned *cand_count;
+// ---- deterministic top-K per plane + fixed-size list
+struct SelectParams {
+  const unsigned long long *cand_key;
+  const float *cand_pwr;
+  const unsigned *cand_total;
+  const unsigned *cand_count;   // [plane]
   int cand_cap;
-  int per_plane;          // entries per plane in the fixed-size list
+  int n_planes;
+  int per_plane;          // K: entries per plane in the fixed-size list
+  unsigned *hist;         // [plane][kSelBuckets]
+  unsigned *sel_lo;       // [plane] lowest power key taken
+  unsigned long long *sel_key;  // [plane][kSortCap]
+  float *sel_pwr;         // [plane][kSortCap]
+  unsigned *sel_count;    // [plane]
   uint32_t *compat_loc;   // [plane][per_plane]
   float *compat_pwr;
   uint32_t invalid_location;
+  int *status;
 };
 
 // ---- template spectra / taps in FP64
@@ -126,7 +146,7 @@ cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s);
 cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s);
 cudaError_t launch_hsum(const HsumParams &p, cudaStream_t s);
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s);
-cudaError_t launch_finalize(const FinalizeParams &p, int n_planes, cudaStream_t s);
+cudaError_t launch_select(const SelectParams &p, cudaStream_t s);
 cudaError_t launch_spectra(const SpectraParams &p, cudaStream_t s);
 cudaError_t launch_taps(const TapsParams &p, cudaStream_t s);
 

@@ -68,20 +68,37 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, long long timeo
   }
 }
 
-// warp-aggregated append of one record to plane `plane`'s list
-__device__ __forceinline__ void append_candidate(const HsumParams &p, int plane, int row, int bin, float pwr) {
-  const unsigned active = __activemask();
-  const unsigned peers = __match_any_sync(active, plane);
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  unsigned base = 0;
-  if (lane == leader) base = atomicAdd(p.cand_count + plane, (unsigned)__popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  const unsigned idx = base + __popc(peers & ((1u << lane) - 1u));
-  if (idx < (unsigned)p.cand_cap) {
-    const long long o = (long long)plane * p.cand_cap + idx;
-    p.cand_key[o] = ((unsigned long long)(unsigned)row << 32) | (unsigned)bin;
-    p.cand_pwr[o] = pwr;
+// CTA-local candidate staging: records go to shared memory first; the CTA
+// reserves its slice of the global list with one atomic when it finishes.
+struct EmitBuf {
+  unsigned cnt;
+  unsigned base;
+  unsigned pc[kMaxPlanes];
+  unsigned long long key[kEmitBuf];
+  float pwr[kEmitBuf];
+};
+
+__device__ __forceinline__ void global_append(unsigned long long *keys, float *pwrs, unsigned *total, int cap,
+                                              int *status, unsigned long long key, float pwr) {
+  const unsigned g = atomicAdd(total, 1u);
+  if (g < (unsigned)cap) {
+    keys[g] = key;
+    pwrs[g] = pwr;
+  } else {
+    atomicOr(status, kStatusCandidateOverflow);
+  }
+}
+
+__device__ __forceinline__ void emit_candidate(EmitBuf &eb, const HsumParams &p, int plane, int row, int bin,
+                                               float pwr) {
+  atomicAdd(&eb.pc[plane], 1u);
+  const unsigned idx = atomicAdd(&eb.cnt, 1u);
+  const unsigned long long key = cand_key(plane, row, bin);
+  if (idx < (unsigned)kEmitBuf) {
+    eb.key[idx] = key;
+    eb.pwr[idx] = pwr;
+  } else {
+    global_append(p.cand_key, p.cand_pwr, p.cand_total, p.cand_cap, p.status, key, pwr);
   }
 }
 
@@ -106,6 +123,7 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
   extern __shared__ __align__(128) float hs_smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(hs_smem);
   float *stage = hs_smem + 4;
+  EmitBuf &eb = *reinterpret_cast<EmitBuf *>(hs_smem + 4 + ((p.smem_floats + 3) & ~3));
   const int halfsel = blockIdx.y;
   const int sgn = halfsel ? 1 : -1;
   const int tlo = p.tlo[halfsel];
@@ -116,12 +134,16 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
   const int P = p.n_planes;
   const bool staged = p.stage_bytes > 0;
 
-  if (staged) {
-    if (threadIdx.x == 0) {
+  if (threadIdx.x == 0) {
+    eb.cnt = 0;
+    if (staged) {
       mbar_init(bar, 1);
       fence_mbar_init();
     }
-    __syncthreads();
+  }
+  if (threadIdx.x < kMaxPlanes) eb.pc[threadIdx.x] = 0;
+  __syncthreads();
+  if (staged) {
     if (warp == 0) {
       if (lane == 0) mbar_arrive_expect_tx(bar, p.stage_bytes);
       __syncwarp();
@@ -219,11 +241,28 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
               const int a0 = (f0 / j) & ~3;
               a += stage[p.soff[j] + (tk / j) * p.sw[j] + f / j - a0];
             }
-            if (a > p.hi[j - 1]) append_candidate(p, j - 1, row, f, a);
+            if (a > p.hi[j - 1]) emit_candidate(eb, p, j - 1, row, f, a);
             else if (a >= p.lo[j - 1]) append_recheck(p, j - 1, row, f);
           }
         }
       }
+    }
+  }
+
+  // ---- flush the CTA's records with one reservation in the global list
+  __syncthreads();
+  const unsigned n = min(eb.cnt, (unsigned)kEmitBuf);
+  if (threadIdx.x == 0) {
+    eb.base = n ? atomicAdd(p.cand_total, n) : 0u;
+    if (n && eb.base + n > (unsigned)p.cand_cap) atomicOr(p.status, kStatusCandidateOverflow);
+  }
+  if (threadIdx.x < P && eb.pc[threadIdx.x]) atomicAdd(p.cand_count + threadIdx.x, eb.pc[threadIdx.x]);
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+    const unsigned g = eb.base + i;
+    if (g < (unsigned)p.cand_cap) {
+      p.cand_key[g] = eb.key[i];
+      p.cand_pwr[g] = eb.pwr[i];
     }
   }
 }
@@ -260,23 +299,107 @@ __global__ void __launch_bounds__(256) recheck_kernel(RecheckParams p) {
       hp += re * re + im * im;
     }
     if (lane == 0 && hp > p.thr[plane]) {
-      const unsigned idx = atomicAdd(p.cand_count + plane, 1u);
-      if (idx < (unsigned)p.cand_cap) {
-        const long long o = (long long)plane * p.cand_cap + idx;
-        p.cand_key[o] = ((unsigned long long)(unsigned)row << 32) | (unsigned)bin;
-        p.cand_pwr[o] = (float)hp;
+      atomicAdd(p.cand_count + plane, 1u);
+      global_append(p.cand_key, p.cand_pwr, p.cand_total, p.cand_cap, p.status, cand_key(plane, row, bin),
+                    (float)hp);
+    }
+  }
+}
+
+// ------------------------------------------- deterministic top-K per plane
+// The fixed-size list keeps, per plane, the K strongest hits (power
+// descending, location ascending on ties) in location order.  Hits are stored
+// unordered by the harmonic-summing CTAs; the selection is a radix select on
+// the power: a histogram of the top 16 bits of each plane's power keys, the
+// bucket where the count from the top reaches K, a gather of the records at or
+// above that bucket, and a one-CTA sort of the gathered records.
+
+// order-preserving map of a float to an unsigned key
+__device__ __forceinline__ unsigned float_key(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ unsigned stored_records(const SelectParams &p) {
+  return min(*p.cand_total, (unsigned)p.cand_cap);
+}
+
+__global__ void __launch_bounds__(256) select_hist_kernel(SelectParams p) {
+  const unsigned n = stored_records(p);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int plane = (int)(p.cand_key[i] >> 48);
+    if (p.cand_count[plane] > (unsigned)p.per_plane)
+      atomicAdd(p.hist + (size_t)plane * kSelBuckets + (float_key(p.cand_pwr[i]) >> 16), 1u);
+  }
+}
+
+// One CTA (1024 threads) per plane: thread t owns buckets
+// [kSelBuckets - 64 (t+1), kSelBuckets - 64 t), i.e. thread 0 the strongest.
+__global__ void __launch_bounds__(1024) select_threshold_kernel(SelectParams p) {
+  __shared__ unsigned part[1024];
+  __shared__ unsigned found;
+  const int plane = blockIdx.x;
+  unsigned *h = p.hist + (size_t)plane * kSelBuckets;
+  const unsigned K = (unsigned)p.per_plane;
+  if (p.cand_count[plane] <= K) {
+    if (threadIdx.x == 0) p.sel_lo[plane] = 0u;
+    return;
+  }
+  const int t = threadIdx.x;
+  const int hi_b = kSelBuckets - 64 * t;  // exclusive
+  unsigned local = 0;
+  for (int b = hi_b - 64; b < hi_b; ++b) local += h[b];
+  part[t] = local;
+  if (t == 0) found = 0u;
+  __syncthreads();
+  // inclusive scan over threads (strongest first)
+  for (int o = 1; o < 1024; o <<= 1) {
+    const unsigned v = t >= o ? part[t - o] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  const unsigned before = t ? part[t - 1] : 0u;
+  if (before < K && part[t] >= K) {
+    unsigned c = before;
+    int b = hi_b - 1;
+    for (; b >= hi_b - 64; --b) {
+      c += h[b];
+      if (c >= K) break;
+    }
+    p.sel_lo[plane] = (unsigned)b << 16;
+    found = 1u;
+  }
+  __syncthreads();
+  if (t == 0 && !found) p.sel_lo[plane] = 0u;  // fewer stored than K (overflow): take all
+  // leave the histogram zeroed for the next search
+  for (int b = hi_b - 64; b < hi_b; ++b)
+    if (h[b]) h[b] = 0u;
+}
+
+__global__ void __launch_bounds__(256) select_gather_kernel(SelectParams p) {
+  const unsigned n = stored_records(p);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long key = p.cand_key[i];
+    const int plane = (int)(key >> 48);
+    const float pw = p.cand_pwr[i];
+    if (float_key(pw) >= p.sel_lo[plane]) {
+      const unsigned idx = atomicAdd(p.sel_count + plane, 1u);
+      if (idx < (unsigned)kSortCap) {
+        p.sel_key[(size_t)plane * kSortCap + idx] = key;
+        p.sel_pwr[(size_t)plane * kSortCap + idx] = pw;
+      } else {
+        atomicOr(p.status, kStatusSelectionOverflow);
       }
     }
   }
 }
 
-// ----------------------------------------------------------- per-plane sort
 struct Rec {
   unsigned long long key;
   float pwr;
 };
 
-// ascending by key
 __device__ __forceinline__ bool less_key(const Rec &a, const Rec &b) { return a.key < b.key; }
 // "stronger first": power descending, key ascending on ties
 __device__ __forceinline__ bool less_pwr(const Rec &a, const Rec &b) {
@@ -292,9 +415,9 @@ __device__ void bitonic_sort(unsigned long long *keys, float *pwrs, int m) {
         if (ixj > i) {
           Rec a{keys[i], pwrs[i]}, b{keys[ixj], pwrs[ixj]};
           const bool up = (i & k) == 0;
-          const bool b_less = BY_PWR ? less_pwr(b, a) : less_key(b, a);
-          const bool a_less = BY_PWR ? less_pwr(a, b) : less_key(a, b);
-          if (up ? b_less : a_less) {
+          const bool swap = up ? (BY_PWR ? less_pwr(b, a) : less_key(b, a))
+                               : (BY_PWR ? less_pwr(a, b) : less_key(a, b));
+          if (swap) {
             keys[i] = b.key; pwrs[i] = b.pwr;
             keys[ixj] = a.key; pwrs[ixj] = a.pwr;
           }
@@ -305,42 +428,35 @@ __device__ void bitonic_sort(unsigned long long *keys, float *pwrs, int m) {
   }
 }
 
-__global__ void __launch_bounds__(1024) finalize_kernel(FinalizeParams p) {
+__global__ void __launch_bounds__(1024) select_finalize_kernel(SelectParams p) {
   extern __shared__ __align__(16) unsigned char fz_smem[];
   const int plane = blockIdx.x;
-  const int n = (int)min(p.cand_count[plane], (unsigned)p.cand_cap);
+  const int n = (int)min(p.sel_count[plane], (unsigned)kSortCap);
   int m = 1;
   while (m < n) m <<= 1;
   unsigned long long *keys = reinterpret_cast<unsigned long long *>(fz_smem);
   float *pwrs = reinterpret_cast<float *>(keys + kSortCap);
-  unsigned long long *gk = p.cand_key + (long long)plane * p.cand_cap;
-  float *gp = p.cand_pwr + (long long)plane * p.cand_cap;
+  const unsigned long long *gk = p.sel_key + (size_t)plane * kSortCap;
+  const float *gp = p.sel_pwr + (size_t)plane * kSortCap;
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     keys[i] = i < n ? gk[i] : ~0ull;
     pwrs[i] = i < n ? gp[i] : -CUDART_INF_F;
-  }
-  __syncthreads();
-  if (n > 1) bitonic_sort<false>(keys, pwrs, m);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    gk[i] = keys[i];
-    gp[i] = pwrs[i];
   }
   __syncthreads();
   int kept = n;
   if (n > p.per_plane) {
     bitonic_sort<true>(keys, pwrs, m);
     kept = p.per_plane;
-    // re-sort the kept strongest by location: pad the rest with max keys
     for (int i = threadIdx.x; i < m; i += blockDim.x)
       if (i >= kept) { keys[i] = ~0ull; pwrs[i] = -CUDART_INF_F; }
     __syncthreads();
-    bitonic_sort<false>(keys, pwrs, m);
   }
-  uint32_t *cl = p.compat_loc + (long long)plane * p.per_plane;
-  float *cp = p.compat_pwr + (long long)plane * p.per_plane;
+  if (kept > 1) bitonic_sort<false>(keys, pwrs, m);
+  uint32_t *cl = p.compat_loc + (size_t)plane * p.per_plane;
+  float *cp = p.compat_pwr + (size_t)plane * p.per_plane;
   for (int i = threadIdx.x; i < p.per_plane; i += blockDim.x) {
     if (i < kept) {
-      const unsigned row = (unsigned)(keys[i] >> 32), bin = (unsigned)(keys[i] & 0xffffffffu);
+      const unsigned row = (unsigned)(keys[i] >> 32) & 0xffffu, bin = (unsigned)(keys[i] & 0xffffffffu);
       // gen_info.h:62-64: ((h-1)&7)<<29 | (row&0x7f)<<22 | (bin&0x3fffff)
       cl[i] = (((unsigned)plane & 7u) << 29) | ((row & 0x7fu) << 22) | (bin & 0x3fffffu);
       cp[i] = pwrs[i];
@@ -352,7 +468,9 @@ __global__ void __launch_bounds__(1024) finalize_kernel(FinalizeParams p) {
 }
 
 // ----------------------------------------------------------------- launchers
-int hsum_smem_bytes(const HsumParams &p) { return 16 + p.smem_floats * 4; }
+int hsum_smem_bytes(const HsumParams &p) {
+  return 16 + ((p.smem_floats + 3) & ~3) * 4 + (int)sizeof(EmitBuf);
+}
 
 template <int MAXP>
 static cudaError_t launch_hsum_t(const HsumParams &p, cudaStream_t s) {
@@ -375,11 +493,14 @@ cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(const FinalizeParams &p, int n_planes, cudaStream_t s) {
+cudaError_t launch_select(const SelectParams &p, cudaStream_t s) {
+  select_hist_kernel<<<4 * 152, 256, 0, s>>>(p);
+  select_threshold_kernel<<<p.n_planes, 1024, 0, s>>>(p);
+  select_gather_kernel<<<4 * 152, 256, 0, s>>>(p);
   const int smem = kSortCap * (8 + 4);
-  cudaError_t e = cudaFuncSetAttribute(finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = cudaFuncSetAttribute(select_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  finalize_kernel<<<n_planes, 1024, smem, s>>>(p);
+  select_finalize_kernel<<<p.n_planes, 1024, smem, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -215,7 +215,7 @@ class FDAS:
         Returns (records, n_total, n_dropped); records has fields harmonic,
         template_num, bin, power."""
         if capacity is None:
-            capacity = self.config.n_planes * (self.config.candidate_capacity or 8192)
+            capacity = self.config.candidate_capacity or (1 << 22)
         out = np.zeros(capacity, dtype=self.CANDIDATE_DTYPE)
         n_total, n_dropped = ctypes.c_uint32(), ctypes.c_uint32()
         ok = self._check(self._lib.fdas_retrieve_candidate_list(self._h, _ptr(out), capacity, ctypes.byref(n_total),

@@ -88,7 +88,7 @@ typedef struct {
   uint32_t max_template_len;   /* 421 in the reference (gen_info.h:28) */
   uint32_t tile_overlap;       /* 0 = ceil((max_template_len - 1) / 4) * 4 (cl_codegen.py:99) */
   uint32_t n_planes;           /* harmonic planes, 1..16 (8 in the reference) */
-  uint32_t candidate_capacity; /* hits kept per plane on the device; 0 = 8192 (max 8192) */
+  uint32_t candidate_capacity; /* hit records kept per buffer set; 0 = 2^22 (max 2^27) */
   uint32_t candidates_per_plane_compat; /* entries per plane in the fixed list; 0 = 512 */
   int32_t device;              /* CUDA device ordinal */
   uint32_t buffer_mode;        /* fdas_buffer_mode */
@@ -184,7 +184,7 @@ typedef struct {
 /* Every hit of the last harmonic summing on `ab`, sorted by (harmonic,
  * template, bin) -- the order of hsum.py's list.  Writes min(total, capacity)
  * records; *n_total gets the number of hits found, *n_dropped the hits lost to
- * the device capacity (candidate_capacity per plane).  Blocking. */
+ * the device capacity (candidate_capacity records per set).  Blocking. */
 fdas_status fdas_retrieve_candidate_list(fdas_handle *h, fdas_candidate *out, uint32_t capacity,
                                          uint32_t *n_total, uint32_t *n_dropped, fdas_buffer_set ab);
 

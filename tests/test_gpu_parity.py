@@ -20,7 +20,17 @@ from oracle import fdas_oracle as O
 
 pytestmark = pytest.mark.gpu
 
-FOP_REL_TOL = 1e-5  # |FOP_gpu - FOP_fp64| <= 1e-5 * mean power of the plane
+# FOP tolerance against the FP64 oracle: 1e-5 of the plane's mean power, plus
+# 1e-6 of the cell's own power.  The second term only matters at strong
+# signals: there a float32 FOP value cannot be stored closer than half an ulp
+# (3e-8 relative), which for a cell 300x the mean is already 1e-5 of the mean.
+FOP_REL_TOL = 1e-5
+FOP_VALUE_TOL = 1e-6
+
+
+def fop_within(fop, ref):
+    mean = ref.mean(axis=-1, keepdims=True)
+    return np.abs(fop - ref) <= FOP_REL_TOL * mean + FOP_VALUE_TOL * np.abs(ref)
 
 
 @pytest.fixture(scope="module")
@@ -68,9 +78,11 @@ def test_fop_vs_fp64_oracle(name, layout, bank64, bank_p4):
     lay = FDAS.TemplatesFFTP4 if layout == "p4" else FDAS.TemplatesTimeDomain
     _, _, fop = run_ftc(g["input"], bank, lay)
     ref = O.fop(g["input"], bank64)
+    assert fop_within(fop, ref).all()
+    # the plain 1e-5-of-mean bound holds for every cell below 30x the mean power
     mean = ref.mean(axis=1, keepdims=True)
-    err = np.abs(fop - ref) / mean
-    assert err.max() <= FOP_REL_TOL, err.max()
+    weak = ref < 30 * mean
+    assert (np.abs(fop - ref)[weak] <= FOP_REL_TOL * np.broadcast_to(mean, ref.shape)[weak]).all()
     # main_gtest.cpp:183-190 absolute check against the reference's own FOP
     assert np.abs(fop[g["fop_rows"]] - g["fop_ref"]).max() < 1e-5
 
@@ -82,7 +94,7 @@ def test_fop_part_rows_only(part, bank_p4):
     rows = np.arange(0, 43) if part == FDAS.NegativeAccelerations else np.arange(42, 85)
     other = np.setdiff1d(np.arange(85), rows)
     ref = O.fop(g["input"], template_bank(), rows=rows)
-    assert np.abs(fop[rows] - ref).max() <= FOP_REL_TOL * ref.mean()
+    assert fop_within(fop[rows], ref).all()
     assert np.all(fop[other] == 0)  # untouched rows of a fresh buffer set
 
 
@@ -156,7 +168,7 @@ def test_search_candidates_equal_fp64_oracle(name, thr_key, layout, bank64, bank
     common = np.isin(gl, ol)
     ref_p = dict(zip(ol.tolist(), op.tolist()))
     rp = np.array([ref_p[x] for x in gl[common].tolist()])
-    assert np.all(np.abs(gp[common] - rp) <= 8 * FOP_REL_TOL * fop64.mean() + 1e-6 * np.abs(rp))
+    assert np.all(np.abs(gp[common] - rp) <= 8 * FOP_REL_TOL * fop64.mean() + 8 * FOP_VALUE_TOL * np.abs(rp))
     # the fixed-size list holds the strongest per plane, as the oracle's rule says
     cl, cp = O.compat_list(ol, op.astype(np.float32), (ol >> 29).astype(np.int64))
     if layout == "time":
@@ -174,16 +186,20 @@ def test_candidate_capacity_and_compat_overflow():
     rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
     hps = O.harmonic_planes(g["fop_ref"].astype(np.float32), 8, dtype=np.float32)
     ol, op, opl, *_ = O.detections(hps, thr)
-    assert total == ol.size
-    if dropped == 0:
-        loc, pwr = candidates_as_arrays(rec)
-        assert np.array_equal(loc, ol) and np.array_equal(pwr, op)
+    assert total == ol.size and dropped == 0
+    loc, pwr = candidates_as_arrays(rec)
+    assert np.array_equal(loc, ol) and np.array_equal(pwr, op)
     cloc = np.zeros(4096, dtype=np.uint32)
     cpwr = np.zeros(4096, dtype=np.float32)
     assert p.retrieve_candidates(cloc, cpwr, FDAS.A)
     el, ep = O.compat_list(ol, op, opl)
-    if dropped == 0:
-        assert np.array_equal(cloc, el) and np.array_equal(cpwr, ep)
+    assert np.array_equal(cloc, el) and np.array_equal(cpwr, ep)
+    # a capacity below the number of hits is reported, not silently truncated
+    q = make_pipeline(4096, log=io.StringIO(), candidate_capacity=1000)
+    assert q.inject_FOP(g["fop_ref"], FDAS.A)
+    assert q.perform_harmonic_summing(thr, FDAS.AllAccelerations, FDAS.A)
+    rec, total, dropped = q.retrieve_candidate_list(FDAS.A)
+    assert total == ol.size and dropped == ol.size - 1000 and rec.size == 1000
 
 
 def _drive(sync_pipeline, n_runs=4):
@@ -254,7 +270,7 @@ def test_edge_sizes(n_bins, bank64):
     fop = np.zeros(p.get_fop_sz(), dtype=np.float32)
     assert p.retrieve_FOP(fop, FDAS.A)
     ref = O.fop(x, bank64)
-    assert np.abs(fop.reshape(85, n_bins) - ref).max() <= FOP_REL_TOL * max(ref.mean(), 1e-30)
+    assert fop_within(fop.reshape(85, n_bins), ref).all()
     rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
     gl, _ = candidates_as_arrays(rec)
     ol, *_ = O.detections(O.harmonic_planes(ref, 8, dtype=np.float64), thr)
@@ -294,13 +310,7 @@ def test_full_size_properties(bank64):
     assert p.retrieve_FOP(fop, FDAS.A)
     fop = fop.reshape(85, n)
     fop64 = O.fop(x, bank64)
-    mean = fop64.mean(axis=1, keepdims=True)
-    # strong injected signals make FP32 rounding of the largest cells exceed
-    # 1e-5 of the mean; the bound used is 1e-5 of the mean plus 2^-20 relative
-    err = np.abs(fop - fop64)
-    assert np.all(err <= FOP_REL_TOL * mean + 2.0 ** -20 * np.abs(fop64))
-    noise_rows = err / mean
-    assert np.median(noise_rows.max(axis=1)) <= FOP_REL_TOL
+    assert fop_within(fop, fop64).all()
     rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
     assert dropped == 0
     gl, gp = candidates_as_arrays(rec)
