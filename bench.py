@@ -125,7 +125,7 @@ def cpu_fop_rows(args):
     return O.fop(x, bank, dtype=dtype, rows=rows)
 
 
-def cpu_search_time(x, bank, thr, n_rows_sample, bin_frac, dtype, workers=1):
+def cpu_search_time(x, bank, thr, n_rows_sample, bin_frac, dtype, pool=None, workers=1):
     """Extrapolated time of one CPU search from a bounded sample.
 
     FOP: ``n_rows_sample`` of the 85 rows by direct linear convolution (scaled
@@ -136,11 +136,9 @@ def cpu_search_time(x, bank, thr, n_rows_sample, bin_frac, dtype, workers=1):
     from oracle import fdas_oracle as O
     rows = np.linspace(0, N_TEMPLATES - 1, n_rows_sample).astype(int)
     t0 = time.perf_counter()
-    if workers > 1:
-        import multiprocessing as mp
+    if pool is not None:
         chunks = np.array_split(rows, workers)
-        with mp.get_context("spawn").Pool(workers) as pool:
-            pool.map(cpu_fop_rows, [(x, bank, list(c), dtype) for c in chunks if len(c)])
+        pool.map(cpu_fop_rows, [(x, bank, list(c), dtype) for c in chunks if len(c)])
     else:
         O.fop(x, bank, dtype=dtype, rows=rows)
     t_fop = (time.perf_counter() - t0) * N_TEMPLATES / n_rows_sample
@@ -156,11 +154,11 @@ def cpu_search_time(x, bank, thr, n_rows_sample, bin_frac, dtype, workers=1):
     return t_fop + t_hs, desc
 
 
-def make_inputs():
+def make_inputs(n_bins=N_BINS):
     from fdas_gb300 import synth
     from fdas_gb300.templates import template_bank
     samples, _ = synth.full_case()
-    x, _ = synth.spectrum(samples)
+    x, _ = synth.spectrum(samples[:2 * n_bins])
     bank = template_bank()
     from scipy.stats import gamma
     thr = np.array([gamma.isf(1e-6, k) for k in range(1, N_PLANES + 1)], dtype=np.float32)
@@ -176,11 +174,15 @@ def run_reference(args):
     workers = os.cpu_count() or 1
     times = []
     desc = ""
-    for i in range(args.warmup + args.steps):
-        t, desc = cpu_search_time(x, bank, thr, n_rows_sample=min(N_TEMPLATES, 2 * workers), bin_frac=1 / 16,
-                                  dtype=np.float32, workers=workers)
-        if i >= args.warmup:
-            times.append(t)
+    import multiprocessing as mp
+    # one row per worker and 1/64 of the bins per step keeps a step near half
+    # a second on 16 cores, so --steps K --warmup W ends within minutes
+    with mp.get_context("spawn").Pool(workers) as pool:
+        for i in range(args.warmup + args.steps):
+            t, desc = cpu_search_time(x, bank, thr, n_rows_sample=min(N_TEMPLATES, workers), bin_frac=1 / 64,
+                                      dtype=np.float32, pool=pool, workers=workers)
+            if i >= args.warmup:
+                times.append(t)
     v = 1.0 / float(np.mean(times))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
@@ -201,10 +203,11 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from fdas_gb300.fdas import FDAS, PinnedArray
 
-    x, bank, thr = make_inputs()
+    n_bins = args.bins
+    x, bank, thr = make_inputs(n_bins)
     log = open(os.devnull, "w")
     p = FDAS(log)
-    assert p.initialise_accelerator(N_BINS, device=local), p.last_error
+    assert p.initialise_accelerator(n_bins, device=local), p.last_error
     assert p.upload_templates(bank, FDAS.A), p.last_error
     assert p.upload_templates(bank, FDAS.B), p.last_error
     d_x = torch.from_numpy(x.view(np.float32)).to(f"cuda:{local}")
@@ -242,7 +245,9 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = ws * args.steps / (total_ms / 1e3)
-    rec, n_cand, dropped = p.retrieve_candidate_list(FDAS.A)
+    counters = p.counters(FDAS.A)
+    n_cand = sum(counters["per_plane"])
+    dropped = max(0, n_cand - counters["records"])
 
     # ---- stage times (separate pass, so the per-launch host syncs do not
     # disturb the throughput number above)
@@ -254,8 +259,8 @@ def run_ours(args):
     st = np.array(st)
     names = ["input", "tiling", "ft_convolution", "harmonic_summing", "download", "total"]
     stage_ms = {n: float(np.mean(st[:, i])) for i, n in enumerate(names)}
-    alg = {"tiling": 8 * N_BINS, "ft_convolution": 4 * N_TEMPLATES * N_BINS,
-           "harmonic_summing": 4 * N_TEMPLATES * N_BINS}
+    alg = {"tiling": 8 * n_bins, "ft_convolution": 4 * N_TEMPLATES * n_bins,
+           "harmonic_summing": 4 * N_TEMPLATES * n_bins}
     dom = max(alg, key=lambda k: stage_ms[k])
     peak, peak_kind = measured_peaks()
     achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9
@@ -265,7 +270,12 @@ def run_ours(args):
         traffic = json.loads(tf.read_text()).get(dom)
 
     # ---- e2e: pinned host buffers through fdas_launch / fdas_wait, A/B sets
-    hx = {ab: PinnedArray((N_BINS,), np.complex64) for ab in (FDAS.A, FDAS.B)}
+    if args.no_e2e:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_bins": n_bins,
+                              "stage_ms": stage_ms, "counters": counters, "profile_run": True}), flush=True)
+        return
+    hx = {ab: PinnedArray((n_bins,), np.complex64) for ab in (FDAS.A, FDAS.B)}
     for ab in hx:
         hx[ab].array[:] = x
     n_list = p.get_candidate_list_sz()
@@ -309,10 +319,11 @@ def run_ours(args):
         "dtype": "f32", "data": "synthetic", "config": dict(WORKLOAD, parallelism=f"replicas{ws}"),
         "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
         "stage_ms": stage_ms, "candidates": int(n_cand), "candidates_dropped": int(dropped),
+        "recheck_cells": counters["recheck"], "device_status": counters["status"],
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": alg[dom], "traffic": traffic},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * N_BINS,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n_bins,
                 "d2h_bytes_per_step": 8 * n_list},
         "gpu_launches": launches_per_search * args.steps,
         "clocks": clocks.summary(),
@@ -329,6 +340,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--stage-times", action="store_true", help="per-step stage events inside the timed loop")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="device-resident leg only (profiling runs)")
+    ap.add_argument("--bins", type=int, default=N_BINS,
+                    help="spectrum bins; the reported workload is 2^21, smaller values are for ncu captures")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -35,40 +35,46 @@ __global__ void __launch_bounds__(256) tile_fft_kernel(TileParams p) {
   });
 }
 
-// One warp per (tile, template).  Y = S_tile * T_tmpl (templates carry the
-// 1/2048 of the inverse transform, so |y|^2 already includes the reference's
-// power normalisation by 2048^2, utils.cl.mako:41-47); y = IFFT(Y);
+// Persistent: one CTA of 8 warps per SM; each warp loops over (tile,
+// template) items, item = tile * n_rows + r, so the 8 warps of a CTA usually
+// share the tile operand in L1 while their phases drift apart (one warp's
+// loads overlap the others' arithmetic).
+// Per item: Y = S_tile * T_tmpl (templates carry the 1/2048 of the inverse
+// transform, so |y|^2 already includes the reference's power normalisation by
+// 2048^2, utils.cl.mako:41-47); y = IFFT(Y);
 // FOP[row][i P + n - O] = |y[n]|^2 for n >= O, trimmed to N bins
 // (square_and_discard.cl.mako:28-76).
 __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
   extern __shared__ float4 smem_f4[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile = blockIdx.x;
-  const int rloc = blockIdx.y * kWarpsPerCta + warp;
-  if (rloc >= p.n_rows) return;
-  const int row = p.row_begin + rloc;
   float *ex = reinterpret_cast<float *>(smem_f4) + warp * kExFloats;
   const TwiddleBases tb = load_twiddle_bases<+1>(p.twiddle, lane);
-  const float2 *s = p.tiles + (long long)tile * kTile + lane;
-  const float2 *t = p.tmpl + (long long)row * kTile + lane;
-  float2 v[64];
-  sfor<64>([&](auto K) {
-    constexpr int k = decltype(K)::value;
-    v[k] = cmul(__ldg(s + 32 * k), __ldg(t + 32 * k));
-  });
-  ifft2048_core(v, tb, ex, lane);
-  float *out = p.fop + (long long)row * p.fop_stride;
-  const long long base = (long long)tile * p.payload - p.overlap;
-  sfor<2>([&](auto C) {
-    constexpr int c = decltype(C)::value;
-    sfor<32>([&](auto D) {
-      constexpr int d = decltype(D)::value;
-      const int n = lane + 32 * c + 64 * d;
-      const long long b = base + n;
-      const float2 y = v[32 * c + pos32(d)];
-      if (n >= p.overlap && b < p.n_bins) out[b] = fmaf(y.x, y.x, y.y * y.y);
+  const long long n_items = (long long)p.n_tiles * p.n_rows;
+  const long long stride = (long long)gridDim.x * kWarpsPerCta;
+  for (long long item = (long long)blockIdx.x * kWarpsPerCta + warp; item < n_items; item += stride) {
+    const int tile = (int)(item / p.n_rows);
+    const int row = p.row_begin + (int)(item - (long long)tile * p.n_rows);
+    const float2 *s = p.tiles + (long long)tile * kTile + lane;
+    const float2 *t = p.tmpl + (long long)row * kTile + lane;
+    float2 v[64];
+    sfor<64>([&](auto K) {
+      constexpr int k = decltype(K)::value;
+      v[k] = cmul(__ldg(s + 32 * k), __ldg(t + 32 * k));
     });
-  });
+    ifft2048_core(v, tb, ex, lane);
+    float *out = p.fop + (long long)row * p.fop_stride;
+    const long long base = (long long)tile * p.payload - p.overlap;
+    sfor<2>([&](auto C) {
+      constexpr int c = decltype(C)::value;
+      sfor<32>([&](auto D) {
+        constexpr int d = decltype(D)::value;
+        const int n = lane + 32 * c + 64 * d;
+        const long long b = base + n;
+        const float2 y = v[32 * c + pos32(d)];
+        if (n >= p.overlap && b < p.n_bins) out[b] = fmaf(y.x, y.x, y.y * y.y);
+      });
+    });
+  }
 }
 
 // FP64 DFT of the time-domain taps -> float spectra scaled by 2^-11.
@@ -131,8 +137,16 @@ cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
     attr = true;
   }
   if (p.n_rows <= 0 || p.n_tiles <= 0) return cudaSuccess;
-  dim3 grid(p.n_tiles, (p.n_rows + kWarpsPerCta - 1) / kWarpsPerCta);
-  ftc_kernel<<<grid, 256, smem, s>>>(p);
+  static int n_sm = 0;
+  if (!n_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (n_sm <= 0) n_sm = 1;
+  }
+  const long long items = (long long)p.n_tiles * p.n_rows;
+  const long long ctas = (items + kWarpsPerCta - 1) / kWarpsPerCta;
+  ftc_kernel<<<(int)(ctas < n_sm ? ctas : n_sm), 256, smem, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -68,14 +68,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, long long timeo
   }
 }
 
-// CTA-local candidate staging: records go to shared memory first; the CTA
-// reserves its slice of the global list with one atomic when it finishes.
+// Candidate staging: each warp collects its records in a shared-memory
+// buffer (warp ballot -> one slot range per batch) and moves a full buffer to
+// the global list with a single atomic reservation.
+constexpr int kWarpBuf = 128;
+
 struct EmitBuf {
-  unsigned cnt;
-  unsigned base;
-  unsigned pc[kMaxPlanes];
-  unsigned long long key[kEmitBuf];
-  float pwr[kEmitBuf];
+  unsigned pc[kMaxPlanes];                 // hits per plane of this CTA
+  unsigned long long key[8][kWarpBuf];
+  float pwr[8][kWarpBuf];
 };
 
 __device__ __forceinline__ void global_append(unsigned long long *keys, float *pwrs, unsigned *total, int cap,
@@ -89,23 +90,50 @@ __device__ __forceinline__ void global_append(unsigned long long *keys, float *p
   }
 }
 
-__device__ __forceinline__ void emit_candidate(EmitBuf &eb, const HsumParams &p, int plane, int row, int bin,
-                                               float pwr) {
-  atomicAdd(&eb.pc[plane], 1u);
-  const unsigned idx = atomicAdd(&eb.cnt, 1u);
-  const unsigned long long key = cand_key(plane, row, bin);
-  if (idx < (unsigned)kEmitBuf) {
-    eb.key[idx] = key;
-    eb.pwr[idx] = pwr;
-  } else {
-    global_append(p.cand_key, p.cand_pwr, p.cand_total, p.cand_cap, p.status, key, pwr);
+// warp-synchronous: move this warp's staged records to the global list
+__device__ __forceinline__ void warp_flush(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p) {
+  __syncwarp();
+  const int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (lane == 0 && wcount) base = atomicAdd(p.cand_total, wcount);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (unsigned i = lane; i < wcount; i += 32) {
+    const unsigned g = base + i;
+    if (g < (unsigned)p.cand_cap) {
+      p.cand_key[g] = eb.key[warp][i];
+      p.cand_pwr[g] = eb.pwr[warp][i];
+    }
   }
+  if (lane == 0 && wcount && base + wcount > (unsigned)p.cand_cap) atomicOr(p.status, kStatusCandidateOverflow);
+  __syncwarp();
+  wcount = 0;
 }
 
-__device__ __forceinline__ void append_recheck(const HsumParams &p, int plane, int row, int bin) {
-  const unsigned idx = atomicAdd(p.rc_count, 1u);
-  if (idx < (unsigned)p.rc_cap) p.rc_list[idx] = make_uint4((unsigned)plane, (unsigned)row, (unsigned)bin, 0u);
-  else atomicOr(p.status, kStatusRecheckOverflow);
+// warp-synchronous emission of the lanes in `hm` (all lanes call this)
+__device__ __forceinline__ void warp_emit(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
+                                          unsigned hm, int plane, int row, int bin, float pwr) {
+  const int lane = threadIdx.x & 31;
+  const unsigned n = __popc(hm);
+  if (wcount + n > (unsigned)kWarpBuf) warp_flush(eb, warp, wcount, p);
+  if ((hm >> lane) & 1u) {
+    const unsigned slot = wcount + __popc(hm & ((1u << lane) - 1u));
+    eb.key[warp][slot] = cand_key(plane, row, bin);
+    eb.pwr[warp][slot] = pwr;
+  }
+  if (lane == 0) atomicAdd(&eb.pc[plane], n);
+  wcount += n;
+}
+
+__device__ __forceinline__ void warp_recheck(const HsumParams &p, unsigned nm, int plane, int row, int bin) {
+  const int lane = threadIdx.x & 31;
+  unsigned base = 0;
+  if (lane == 0) base = atomicAdd(p.rc_count, (unsigned)__popc(nm));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if ((nm >> lane) & 1u) {
+    const unsigned idx = base + __popc(nm & ((1u << lane) - 1u));
+    if (idx < (unsigned)p.rc_cap) p.rc_list[idx] = make_uint4((unsigned)plane, (unsigned)row, (unsigned)bin, 0u);
+    else atomicOr(p.status, kStatusRecheckOverflow);
+  }
 }
 
 // One CTA per (256-bin block, sign half).  Warp w handles the templates
@@ -135,7 +163,6 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
   const bool staged = p.stage_bytes > 0;
 
   if (threadIdx.x == 0) {
-    eb.cnt = 0;
     if (staged) {
       mbar_init(bar, 1);
       fence_mbar_init();
@@ -168,7 +195,7 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
     trow[k] = tlo + warp + 8 * k;
     if (trow[k] <= H) nk = k + 1;
   }
-  bool flag = false;
+  unsigned long long fmask = 0;  // bit 8k + e: cell needs a closer look
   const int fb = f0 + 4 * lane;
 #pragma unroll
   for (int k = 0; k < KMAX; ++k) {
@@ -184,7 +211,8 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
         acc[k][4 * i + 3] = (f + 3 < p.n_bins) ? q.w : -CUDART_INF_F;
       }
 #pragma unroll
-      for (int e = 0; e < 8; ++e) flag |= acc[k][e] >= p.trig[0];
+      for (int e = 0; e < 8; ++e)
+        if (acc[k][e] >= p.trig[0]) fmask |= 1ull << (8 * k + e);
     }
   }
 
@@ -217,54 +245,50 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
 #pragma unroll
           for (int e = 0; e < 8; ++e) {
             acc[k][e] += rs[off[e]];
-            flag |= acc[k][e] >= tj;
+            if (acc[k][e] >= tj) fmask |= 1ull << (8 * k + e);
           }
         }
       }
     }
   });
 
-  // ---- slow path (rare): recompute flagged lanes' cells in the same order
-  // and emit candidates / recheck entries
-  if (__any_sync(0xffffffffu, flag)) {
-    if (flag) {
-      for (int k = 0; k < nk; ++k) {
-        const int tk = tlo + warp + 8 * k;
-        const int row = H + sgn * tk;
-        const float *rowp = p.fop + (long long)row * p.stride;
-        for (int e8 = 0; e8 < 8; ++e8) {
-          const int f = fb + 128 * (e8 >> 2) + (e8 & 3);
-          if (f >= p.n_bins) continue;
-          float a = rowp[f];
-          for (int j = 1; j <= P; ++j) {
-            if (j > 1) {
-              const int a0 = (f0 / j) & ~3;
-              a += stage[p.soff[j] + (tk / j) * p.sw[j] + f / j - a0];
-            }
-            if (a > p.hi[j - 1]) emit_candidate(eb, p, j - 1, row, f, a);
-            else if (a >= p.lo[j - 1]) append_recheck(p, j - 1, row, f);
-          }
+  // ---- slow path (rare): the warp walks the union of its flagged cells;
+  // every lane recomputes its own cell of that slot in the same order and
+  // emits through warp ballots
+  unsigned long long any = fmask;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) any |= __shfl_xor_sync(0xffffffffu, any, o);
+  unsigned wcount = 0;
+  while (any) {
+    const int b = __ffsll((long long)any) - 1;
+    any &= any - 1;
+    const int k = b >> 3, e = b & 7;
+    const int tk = tlo + warp + 8 * k;
+    const int row = H + sgn * tk;
+    const int f = fb + 128 * (e >> 2) + (e & 3);
+    const bool active = ((fmask >> b) & 1ull) && f < p.n_bins;
+    float a = active ? p.fop[(long long)row * p.stride + f] : 0.f;
+    hs_sfor<MAXP>([&](auto JJ) {
+      constexpr int j = decltype(JJ)::value + 1;
+      if (j <= P) {
+        if constexpr (j > 1) {
+          const int a0 = (f0 / j) & ~3;
+          if (active) a += stage[p.soff[j] + (tk / j) * p.sw[j] + f / j - a0];
         }
+        const bool hit = active && a > p.hi[j - 1];
+        const bool near = active && !hit && a >= p.lo[j - 1];
+        const unsigned hm = __ballot_sync(0xffffffffu, hit);
+        if (hm) warp_emit(eb, warp, wcount, p, hm, j - 1, row, f, a);
+        const unsigned nm = __ballot_sync(0xffffffffu, near);
+        if (nm) warp_recheck(p, nm, j - 1, row, f);
       }
-    }
+    });
   }
+  warp_flush(eb, warp, wcount, p);
 
-  // ---- flush the CTA's records with one reservation in the global list
+  // ---- per-plane hit counts of the CTA
   __syncthreads();
-  const unsigned n = min(eb.cnt, (unsigned)kEmitBuf);
-  if (threadIdx.x == 0) {
-    eb.base = n ? atomicAdd(p.cand_total, n) : 0u;
-    if (n && eb.base + n > (unsigned)p.cand_cap) atomicOr(p.status, kStatusCandidateOverflow);
-  }
   if (threadIdx.x < P && eb.pc[threadIdx.x]) atomicAdd(p.cand_count + threadIdx.x, eb.pc[threadIdx.x]);
-  __syncthreads();
-  for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
-    const unsigned g = eb.base + i;
-    if (g < (unsigned)p.cand_cap) {
-      p.cand_key[g] = eb.key[i];
-      p.cand_pwr[g] = eb.pwr[i];
-    }
-  }
 }
 
 // One warp per recheck entry: HP_j of the cell in FP64 from the spectrum and
@@ -489,7 +513,7 @@ cudaError_t launch_hsum(const HsumParams &p, cudaStream_t s) {
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
-  recheck_kernel<<<16, 256, 0, s>>>(p);
+  recheck_kernel<<<2 * 152, 256, 0, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -226,6 +226,16 @@ class FDAS:
         kept = min(int(n_total.value) - int(n_dropped.value), capacity)
         return out[:kept], int(n_total.value), int(n_dropped.value)
 
+    def counters(self, ab):
+        """Device counters of the last harmonic summing: dict with status,
+        recheck (cells sent to the FP64 recheck), records and per-plane hits."""
+        out = np.zeros(19, dtype=np.uint32)
+        if not self._check(self._lib.fdas_get_counters(self._h, int(ab), _ptr(out)), "get_counters"):
+            return None
+        n = self.config.n_planes
+        return {"status": int(out[0]), "recheck": int(out[1]), "records": int(out[2]),
+                "per_plane": [int(x) for x in out[3:3 + n]]}
+
     def stage_times(self, ab):
         ms = np.zeros(6, dtype=np.float32)
         ok = self._check(self._lib.fdas_get_stage_times(self._h, int(ab), _ptr(ms)), "get_stage_times")

@@ -340,3 +340,28 @@ def hp_cells(fop_plane, plane, rows, bins, dtype=np.float64):
             acc = dtype(acc + dtype(f[subharmonic_row(int(r), k, n_tmpl), int(b) // k]))
         out[i] = acc
     return out
+
+
+def harmonic_planes_streaming_error(fop32, fop64, thresholds, n_planes=8, window=(0.5, 2.0)):
+    """max |HP32 - HP64| / thr over cells whose FP64 harmonic sum lies within
+    ``window`` x thr, with HP32 accumulated in float32 from ``fop32`` in the
+    kernel's order and HP64 in float64 from ``fop64`` (full-size, streaming)."""
+    f32 = np.asarray(fop32, dtype=np.float32)
+    f64 = np.asarray(fop64, dtype=np.float64)
+    n_tmpl, n_freq = f32.shape
+    rows = np.arange(n_tmpl)
+    freqs = np.arange(n_freq)
+    h32 = f32.copy()
+    h64 = f64.copy()
+    worst = 0.0
+    for h in range(n_planes):
+        k = h + 1
+        if k > 1:
+            sr = subharmonic_row(rows, k, n_tmpl)
+            h32 += f32[sr][:, freqs // k]
+            h64 += f64[sr][:, freqs // k]
+        thr = float(thresholds[h])
+        sel = (h64 > window[0] * thr) & (h64 < window[1] * thr)
+        if sel.any():
+            worst = max(worst, float(np.max(np.abs(h32[sel].astype(np.float64) - h64[sel])) / thr))
+    return worst

@@ -259,7 +259,7 @@ def test_drive_pipelined():
 def test_edge_sizes(n_bins, bank64):
     """Ragged sizes: a single bin, a partial first tile, exact tile multiples."""
     rng = np.random.default_rng(n_bins)
-    x = (rng.standard_normal(n_bins) + 1j * rng.standard_normal(n_bins)).astype(np.complex64) / np.sqrt(2)
+    x = ((rng.standard_normal(n_bins) + 1j * rng.standard_normal(n_bins)) / np.sqrt(2)).astype(np.complex64)
     p = make_pipeline(n_bins, log=io.StringIO())
     assert p.upload_templates(bank64, FDAS.A)
     thr = O.chi2_thresholds(1e-3)
@@ -316,6 +316,13 @@ def test_full_size_properties(bank64):
     gl, gp = candidates_as_arrays(rec)
     ol, op, *_ = O.detections_streaming(fop64, thr)
     assert np.array_equal(gl, ol)
+    cnt = p.counters(FDAS.A)
+    assert cnt["status"] == 0 and cnt["records"] == total
+    # margin of the FP32 harmonic sums against the FP64 ones, relative to the
+    # threshold, over all cells near a threshold: the recheck band must cover it
+    hp32 = O.harmonic_planes_streaming_error(fop, fop64, thr)
+    print("max |HP32 - HP64| / thr near thresholds:", hp32, "recheck cells:", cnt["recheck"])
+    assert hp32 < 1e-4
     # every injected signal is detected near its starting bin
     h, t, f = O.decode_location(gl)
     for s in sig:
