@@ -208,6 +208,8 @@ fdas_status enqueue_ftc(fdas_handle *h, int ab, fdas_fop_part which) {
   p.payload = h->payload;
   rows_of(h, which, &p.row_begin, &p.n_rows);
   p.twiddle = h->d_twiddle;
+  p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlStatus);
+  p.timeout_ns = 2000000000LL;  // 2 s
   CK(h, launch_ftc(p, S.stream));
   CK(h, cudaEventRecord(S.ev[3], S.stream));
   S.ev_ftc_recorded = true;
@@ -251,9 +253,10 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   }
   int off = 0;
   unsigned bytes = 0;
+  const int groups = (H + 1 + 3) / 4;  // the kernel's warps own |t| = 4w .. 4w+3
   for (int j = 2; j <= P; ++j) {
-    p.srows[j] = H / j + 1;
-    p.sw[j] = ((kHsBins - 1) / j + 5 + 3) & ~3;
+    p.srows[j] = (4 * groups - 1) / j + 2;  // + one spare row for the 2 x 2 windows
+    p.sw[j] = ((kHsBins - 1) / j + 6 + 3) & ~3;  // + 2x2-window spare column
     p.soff[j] = off;
     off += p.srows[j] * p.sw[j];
     bytes += (unsigned)(p.srows[j] * p.sw[j] * 4);

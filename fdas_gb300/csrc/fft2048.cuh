@@ -231,10 +231,17 @@ __device__ __forceinline__ TwiddleBases load_twiddle_bases(const float2 *__restr
   return tb;
 }
 
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
 // Inverse transform core: v[64] holds Y[32 k' + lane] at v[k'] on entry.  On
 // exit v[32 c + pos32(d)] holds y[lane + 32 c + 64 d].  ``ex`` is this warp's
-// exchange buffer (kExFloats floats, 16-byte aligned).
-__device__ __forceinline__ void ifft2048_core(float2 *v, const TwiddleBases &tb, float *ex, int lane) {
+// exchange buffer (kExFloats floats, 16-byte aligned); ``after_exchange`` runs
+// (on all lanes) once the buffer has been read back and is free again.
+template <typename Hook = NoHook>
+__device__ __forceinline__ void ifft2048_core(float2 *v, const TwiddleBases &tb, float *ex, int lane,
+                                              Hook after_exchange = Hook()) {
   dft64<+1, 0>(v);
   // twiddle V[m] = Z[m] w^(m lane);  Z[m] sits at v[pos64(m)] = v[8 mlo + mhi]
   sfor<8>([&](auto MLO) {
@@ -253,6 +260,7 @@ __device__ __forceinline__ void ifft2048_core(float2 *v, const TwiddleBases &tb,
     });
   });
   // exchange: row = lane (kappa), column m; 16-byte stores of (m, m+1)
+  __syncwarp();  // every lane is done with whatever the buffer held before
   float4 *row = reinterpret_cast<float4 *>(ex + 2 * kExPitch * lane);
   sfor<32>([&](auto P) {
     constexpr int p = decltype(P)::value;  // m = 2p, 2p+1
@@ -269,6 +277,7 @@ __device__ __forceinline__ void ifft2048_core(float2 *v, const TwiddleBases &tb,
     });
   });
   __syncwarp();
+  after_exchange();
   dft32<+1, 0>(v);
   dft32<+1, 32>(v);
 }

@@ -9,7 +9,6 @@ namespace fdas {
 constexpr int kTile = 2048;          // FFT / tile size (gen_info.h:33, 42)
 constexpr int kMaxPlanes = 16;       // harmonic planes supported by the kernels
 constexpr int kHsBins = 256;         // bins per harmonic-summing CTA
-constexpr int kHsThreads = 256;
 constexpr int kSortCap = 8192;       // records one CTA sorts in shared memory
 constexpr int kEmitBuf = 1024;       // candidate records staged per harmonic-summing CTA
 constexpr int kSelBuckets = 65536;   // power buckets of the top-K selection (top 16 key bits)
@@ -19,6 +18,7 @@ constexpr int kStatusHsumTimeout = 1;
 constexpr int kStatusRecheckOverflow = 2;
 constexpr int kStatusCandidateOverflow = 4;
 constexpr int kStatusSelectionOverflow = 8;
+constexpr int kStatusFtcTimeout = 16;
 
 // Candidate record key: plane << 48 | row << 32 | bin.  Ascending key order is
 // (harmonic, template, bin) -- the order of hsum.py's list.
@@ -51,6 +51,8 @@ struct FtcParams {
   int row_begin;          // first FOP row of the part
   int n_rows;             // rows of the part
   const float2 *twiddle;
+  int *status;
+  long long timeout_ns;
 };
 
 // ---- (d) harmonic summing + thresholds + candidate compaction (preload,
@@ -67,7 +69,7 @@ struct HsumParams {
   float lo[kMaxPlanes];   // recheck if lo <= HP <= hi (lo = +inf: never)
   int sw[kMaxPlanes + 1];   // staged row width (floats) of plane j
   int soff[kMaxPlanes + 1]; // offset (floats) of plane j's staging block
-  int srows[kMaxPlanes + 1];// rows staged for plane j (= half / j + 1)
+  int srows[kMaxPlanes + 1];// rows staged for plane j
   unsigned stage_bytes;   // total bytes moved by the bulk copies
   int smem_floats;        // staging floats (after the 16-byte barrier slot)
   unsigned long long *cand_key;  // [cap] records, any order

@@ -35,10 +35,57 @@ __global__ void __launch_bounds__(256) tile_fft_kernel(TileParams p) {
   });
 }
 
+// ------------------------------------------------------------ TMA helpers
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long timeout_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = gtimer();
+  while (!mbar_try_wait(bar, parity))
+    if ((long long)(gtimer() - t0) > timeout_ns) return false;
+  return true;
+}
+// 16 KB template spectrum -> this warp's exchange buffer (async proxy)
+__device__ __forceinline__ void prefetch_template(float *ex, const float2 *src, uint64_t *bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_arrive_expect_tx(bar, kTile * 8);
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(ex)),
+      "l"(src), "r"((uint32_t)(kTile * 8)), "r"(smem_addr(bar))
+      : "memory");
+}
+
 // Persistent: one CTA of 8 warps per SM; each warp loops over (tile,
 // template) items, item = tile * n_rows + r, so the 8 warps of a CTA usually
-// share the tile operand in L1 while their phases drift apart (one warp's
-// loads overlap the others' arithmetic).
+// share the tile operand in L1 while their phases drift apart.  The next
+// item's template spectrum is prefetched by a 16 KB TMA bulk copy into the
+// warp's exchange buffer as soon as the exchange has been read back, so it
+// lands during the second FFT pass.
 // Per item: Y = S_tile * T_tmpl (templates carry the 1/2048 of the inverse
 // transform, so |y|^2 already includes the reference's power normalisation by
 // 2048^2, utils.cl.mako:41-47); y = IFFT(Y);
@@ -46,22 +93,47 @@ __global__ void __launch_bounds__(256) tile_fft_kernel(TileParams p) {
 // (square_and_discard.cl.mako:28-76).
 __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
   extern __shared__ float4 smem_f4[];
+  __shared__ uint64_t bars[kWarpsPerCta];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float *ex = reinterpret_cast<float *>(smem_f4) + warp * kExFloats;
+  uint64_t *bar = &bars[warp];
+  const int n_items = p.n_tiles * p.n_rows;
+  const int stride = gridDim.x * kWarpsPerCta;
+  int item = blockIdx.x * kWarpsPerCta + warp;
+  if (lane == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
   const TwiddleBases tb = load_twiddle_bases<+1>(p.twiddle, lane);
-  const long long n_items = (long long)p.n_tiles * p.n_rows;
-  const long long stride = (long long)gridDim.x * kWarpsPerCta;
-  for (long long item = (long long)blockIdx.x * kWarpsPerCta + warp; item < n_items; item += stride) {
-    const int tile = (int)(item / p.n_rows);
-    const int row = p.row_begin + (int)(item - (long long)tile * p.n_rows);
+  if (item < n_items && lane == 0)
+    prefetch_template(ex, p.tmpl + (long long)(p.row_begin + item % p.n_rows) * kTile, bar);
+  uint32_t parity = 0;
+  for (; item < n_items; item += stride) {
+    const int tile = item / p.n_rows;
+    const int row = p.row_begin + (item - tile * p.n_rows);
     const float2 *s = p.tiles + (long long)tile * kTile + lane;
-    const float2 *t = p.tmpl + (long long)row * kTile + lane;
     float2 v[64];
     sfor<64>([&](auto K) {
       constexpr int k = decltype(K)::value;
-      v[k] = cmul(__ldg(s + 32 * k), __ldg(t + 32 * k));
+      v[k] = __ldg(s + 32 * k);
     });
-    ifft2048_core(v, tb, ex, lane);
+    if (!mbar_wait(bar, parity, p.timeout_ns)) {
+      if (lane == 0) atomicOr(p.status, kStatusFtcTimeout);
+      mbar_wait(bar, parity, p.timeout_ns);  // bounded: let the copy land before exiting
+      return;
+    }
+    parity ^= 1u;
+    const float2 *t = reinterpret_cast<const float2 *>(ex) + lane;
+    sfor<64>([&](auto K) {
+      constexpr int k = decltype(K)::value;
+      v[k] = cmul(v[k], t[32 * k]);
+    });
+    const int next = item + stride;
+    ifft2048_core(v, tb, ex, lane, [&]() {
+      if (next < n_items && lane == 0)
+        prefetch_template(ex, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
+    });
     float *out = p.fop + (long long)row * p.fop_stride;
     const long long base = (long long)tile * p.payload - p.overlap;
     sfor<2>([&](auto C) {

@@ -71,12 +71,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, long long timeo
 // Candidate staging: each warp collects its records in a shared-memory
 // buffer (warp ballot -> one slot range per batch) and moves a full buffer to
 // the global list with a single atomic reservation.
-constexpr int kWarpBuf = 128;
+constexpr int kWarpBuf = 64;
+constexpr int kHsMaxWarps = 16;  // templates per half <= 64
 
 struct EmitBuf {
   unsigned pc[kMaxPlanes];                 // hits per plane of this CTA
-  unsigned long long key[8][kWarpBuf];
-  float pwr[8][kWarpBuf];
+  unsigned long long key[kHsMaxWarps][kWarpBuf];
+  float pwr[kHsMaxWarps][kWarpBuf];
 };
 
 __device__ __forceinline__ void global_append(unsigned long long *keys, float *pwrs, unsigned *total, int cap,
@@ -136,18 +137,58 @@ __device__ __forceinline__ void warp_recheck(const HsumParams &p, unsigned nm, i
   }
 }
 
-// One CTA per (256-bin block, sign half).  Warp w handles the templates
-// |t| = tlo + w + 8k of the half; lane l the bins f0 + 4 l + 128 i + e
-// (i < 2, e < 4).  For plane j >= 2 the rows trunc(t / j) and bins
+// One CTA per (256-bin block, sign half), one warp per group of 4 templates:
+// warp w owns |t| = 4w + k (k < 4), lane l the bins f0 + 128 i + 4 l + e
+// (i < 2, e < 4), so every thread holds a 4 x 4 tile of cells aligned to 4 in
+// both directions.  For planes j >= 2 the rows trunc(t/j) and bins
 // [f0/j, (f0+255)/j] of the half are staged in shared memory by TMA bulk
-// copies; plane 1 is read straight from global memory.
+// copies (one per plane and row, 16-byte aligned); plane 1 is read from global
+// memory with 128-bit loads.  With the tile aligned to 4, planes 2, 4 and 8
+// map the 4 x 4 tile onto 2 x 2, 1 x 1 and 1 x 1 staged values at
+// compile-time offsets; planes 3, 5, 6, 7 onto a 2 x 2 window whose split
+// points are computed once per thread.
 //
 // HP_1 = FOP[t][f], HP_j = HP_{j-1} + FOP[trunc(t/j)][f/j] accumulated in FP32
 // in this order -- hsum.py:95-120 / hms_baseline.cl.mako:55-84 -- so the
 // values match hsum.py bit for bit for the same FOP.  A cell is a candidate of
-// plane j if HP_j > thr_j (strict, hsum.py:134 / detect.cl.mako:185).
+// plane j if HP_j > thr_j (strict, hsum.py:134 / detect.cl.mako:185).  The fast
+// path only records, per thread, whether any cell reached the lower edge of a
+// threshold band; such warps re-walk their cells warp-synchronously and emit
+// through ballots.
+struct HsGeom {
+  const float *stage;
+  int f0, w, lane;
+};
+
+// value of plane j (>= 2) for cell (k, e) of this thread's tile, from the staged rows
+template <int J>
+struct PlaneWindow {
+  float v00, v01, v10, v11;
+  int kstar, estar;
+  __device__ __forceinline__ void load(const HsumParams &p, const HsGeom &g, int F) {
+    const int a0 = (g.f0 / J) & ~3;
+    const float *blk = g.stage + p.soff[J];
+    const int sw = p.sw[J];
+    const int t0 = 4 * g.w;
+    const int rb = t0 / J;
+    kstar = J - (t0 - rb * J);     // first k with trunc((t0+k)/J) = rb + 1
+    const int bb = F / J;
+    estar = J - (F - bb * J);      // first e with (F+e)/J = bb + 1
+    const float *r0 = blk + rb * sw + (bb - a0);
+    v00 = r0[0];
+    v01 = r0[1];
+    v10 = r0[sw];
+    v11 = r0[sw + 1];
+  }
+  __device__ __forceinline__ float at(int k, int e) const {
+    const float c0 = e < estar ? v00 : v01;
+    const float c1 = e < estar ? v10 : v11;
+    return k < kstar ? c0 : c1;
+  }
+};
+
 template <int MAXP>
-__global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
+__global__ void __launch_bounds__(512) hsum_kernel(HsumParams p) {
   extern __shared__ __align__(128) float hs_smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(hs_smem);
   float *stage = hs_smem + 4;
@@ -158,62 +199,61 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
   const int H = p.half;
   if (tlo > H) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
   const int f0 = blockIdx.x * kHsBins;
   const int P = p.n_planes;
   const bool staged = p.stage_bytes > 0;
 
-  if (threadIdx.x == 0) {
-    if (staged) {
-      mbar_init(bar, 1);
-      fence_mbar_init();
-    }
+  if (threadIdx.x == 0 && staged) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
   }
   if (threadIdx.x < kMaxPlanes) eb.pc[threadIdx.x] = 0;
   __syncthreads();
-  if (staged) {
-    if (warp == 0) {
-      if (lane == 0) mbar_arrive_expect_tx(bar, p.stage_bytes);
-      __syncwarp();
-      for (int j = 2; j <= P; ++j) {
-        const int a0 = (f0 / j) & ~3;
-        const int w = p.sw[j];
-        for (int r = lane; r < p.srows[j]; r += 32) {
-          const float *src = p.fop + (long long)(H + sgn * r) * p.stride + a0;
-          bulk_g2s(stage + p.soff[j] + r * w, src, (uint32_t)w * 4u, bar);
-        }
+  if (staged && warp == 0) {
+    if (lane == 0) mbar_arrive_expect_tx(bar, p.stage_bytes);
+    __syncwarp();
+    for (int j = 2; j <= P; ++j) {
+      const int a0 = (f0 / j) & ~3;
+      const int w = p.sw[j];
+      for (int r = lane; r < p.srows[j]; r += 32) {
+        // rows past |t| = H only feed cells that are masked out; copy row H instead
+        const float *src = p.fop + (long long)(H + sgn * min(r, H)) * p.stride + a0;
+        bulk_g2s(stage + p.soff[j] + r * w, src, (uint32_t)w * 4u, bar);
       }
     }
   }
 
-  // ---- fast path: accumulate all planes, only flag cells at/above trig
-  constexpr int KMAX = 8;  // rows per warp: ceil(64 / 8) covers half <= 63
-  float acc[KMAX][8];
-  int trow[KMAX];
-  int nk = 0;
+  // rows of this warp: |t| = 4 warp + k; invalid ones (|t| > H or < tlo) get -inf
+  const int t0 = 4 * warp;
+  bool rowok[4];
 #pragma unroll
-  for (int k = 0; k < KMAX; ++k) {
-    trow[k] = tlo + warp + 8 * k;
-    if (trow[k] <= H) nk = k + 1;
-  }
-  unsigned long long fmask = 0;  // bit 8k + e: cell needs a closer look
-  const int fb = f0 + 4 * lane;
+  for (int k = 0; k < 4; ++k) rowok[k] = (t0 + k <= H) && (t0 + k >= tlo);
+
+  // plane 1 for both bin sub-blocks (loads in flight while the staging lands)
+  float acc[2][4][4];
 #pragma unroll
-  for (int k = 0; k < KMAX; ++k) {
-    if (k < nk) {
-      const float *rowp = p.fop + (long long)(H + sgn * trow[k]) * p.stride;
+  for (int i = 0; i < 2; ++i) {
+    const int F = f0 + 128 * i + 4 * lane;
 #pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int f = fb + 128 * i;
-        const float4 q = __ldg(reinterpret_cast<const float4 *>(rowp + f));
-        acc[k][4 * i + 0] = (f + 0 < p.n_bins) ? q.x : -CUDART_INF_F;
-        acc[k][4 * i + 1] = (f + 1 < p.n_bins) ? q.y : -CUDART_INF_F;
-        acc[k][4 * i + 2] = (f + 2 < p.n_bins) ? q.z : -CUDART_INF_F;
-        acc[k][4 * i + 3] = (f + 3 < p.n_bins) ? q.w : -CUDART_INF_F;
-      }
-#pragma unroll
-      for (int e = 0; e < 8; ++e)
-        if (acc[k][e] >= p.trig[0]) fmask |= 1ull << (8 * k + e);
+    for (int k = 0; k < 4; ++k) {
+      float4 q = make_float4(-CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F);
+      if (rowok[k]) q = __ldg(reinterpret_cast<const float4 *>(p.fop + (long long)(H + sgn * (t0 + k)) * p.stride + F));
+      acc[i][k][0] = (F + 0 < p.n_bins) ? q.x : -CUDART_INF_F;
+      acc[i][k][1] = (F + 1 < p.n_bins) ? q.y : -CUDART_INF_F;
+      acc[i][k][2] = (F + 2 < p.n_bins) ? q.z : -CUDART_INF_F;
+      acc[i][k][3] = (F + 3 < p.n_bins) ? q.w : -CUDART_INF_F;
     }
+  }
+  bool flag[2] = {false, false};
+  {
+    const float tr = p.trig[0];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) flag[i] |= acc[i][k][e] >= tr;
   }
 
   // the timeout decision is made uniform over the CTA before any warp vote
@@ -221,74 +261,95 @@ __global__ void __launch_bounds__(kHsThreads, 2) hsum_kernel(HsumParams p) {
   if (staged) ok = __syncthreads_and(mbar_wait_bounded(bar, p.timeout_ns)) != 0;
   if (!ok) {
     if (threadIdx.x == 0) atomicOr(p.status, kStatusHsumTimeout);
-    // let copies still in flight land before the CTA exits (bounded again)
-    mbar_wait_bounded(bar, p.timeout_ns);
+    mbar_wait_bounded(bar, p.timeout_ns);  // let copies in flight land (bounded)
     return;
   }
+  const HsGeom g{stage, f0, warp, lane};
 
+  // ---- fast path: planes 2..P, compile-time plane index
   hs_sfor<MAXP - 1>([&](auto JJ) {
     constexpr int j = decltype(JJ)::value + 2;
     if (j <= P) {
-      const int a0 = (f0 / j) & ~3;
-      int off[8];
+      const float tr = p.trig[j - 1];
 #pragma unroll
-      for (int i = 0; i < 2; ++i)
+      for (int i = 0; i < 2; ++i) {
+        const int F = f0 + 128 * i + 4 * lane;
+        if constexpr (j == 2 || j == 4 || j == 8) {
+          const int a0 = (f0 / j) & ~3;
+          const float *blk = stage + p.soff[j] + (F / j - a0);
+          const int sw = p.sw[j];
+          if constexpr (j == 2) {
+            const float2 r0 = *reinterpret_cast<const float2 *>(blk + (t0 / 2) * sw);
+            const float2 r1 = *reinterpret_cast<const float2 *>(blk + (t0 / 2 + 1) * sw);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) off[4 * i + e] = (fb + 128 * i + e) / j - a0;
-      const float *blk = stage + p.soff[j];
-      const int w = p.sw[j];
-      const float tj = p.trig[j - 1];
+            for (int k = 0; k < 4; ++k) {
+              const float2 r = k < 2 ? r0 : r1;
+              acc[i][k][0] += r.x; acc[i][k][1] += r.x; acc[i][k][2] += r.y; acc[i][k][3] += r.y;
+            }
+          } else {
+            const float v = blk[(t0 / j) * sw];
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k) {
-        if (k < nk) {
-          const float *rs = blk + (trow[k] / j) * w;
+            for (int k = 0; k < 4; ++k)
 #pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            acc[k][e] += rs[off[e]];
-            if (acc[k][e] >= tj) fmask |= 1ull << (8 * k + e);
+              for (int e = 0; e < 4; ++e) acc[i][k][e] += v;
           }
+        } else {
+          PlaneWindow<j> win;
+          win.load(p, g, F);
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[i][k][e] += win.at(k, e);
         }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) flag[i] |= acc[i][k][e] >= tr;
       }
     }
   });
 
-  // ---- slow path (rare): the warp walks the union of its flagged cells;
-  // every lane recomputes its own cell of that slot in the same order and
-  // emits through warp ballots
-  unsigned long long any = fmask;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) any |= __shfl_xor_sync(0xffffffffu, any, o);
+  // ---- slow path (rare): warps with a flagged lane re-walk their cells in the
+  // same order; every lane recomputes its own cell and emission goes through
+  // warp ballots into the warp's record buffer
   unsigned wcount = 0;
-  while (any) {
-    const int b = __ffsll((long long)any) - 1;
-    any &= any - 1;
-    const int k = b >> 3, e = b & 7;
-    const int tk = tlo + warp + 8 * k;
-    const int row = H + sgn * tk;
-    const int f = fb + 128 * (e >> 2) + (e & 3);
-    const bool active = ((fmask >> b) & 1ull) && f < p.n_bins;
-    float a = active ? p.fop[(long long)row * p.stride + f] : 0.f;
-    hs_sfor<MAXP>([&](auto JJ) {
-      constexpr int j = decltype(JJ)::value + 1;
-      if (j <= P) {
-        if constexpr (j > 1) {
-          const int a0 = (f0 / j) & ~3;
-          if (active) a += stage[p.soff[j] + (tk / j) * p.sw[j] + f / j - a0];
+  const unsigned flags = (flag[0] ? 1u : 0u) | (flag[1] ? 2u : 0u);
+#pragma unroll 1
+  for (int i = 0; i < 2; ++i) {
+    const bool fl = (flags >> i) & 1u;
+    if (!__any_sync(0xffffffffu, fl)) continue;
+    const int F = f0 + 128 * i + 4 * lane;
+#pragma unroll 1
+    for (int c = 0; c < 16; ++c) {
+      const int k = c >> 2, e = c & 3;
+      const int t = t0 + k;
+      const int f = F + e;
+      const bool active = fl && t <= H && t >= tlo && f < p.n_bins;
+      const int row = H + sgn * t;
+      float a = active ? p.fop[(long long)row * p.stride + f] : 0.f;
+      hs_sfor<MAXP>([&](auto JJ) {
+        constexpr int j = decltype(JJ)::value + 1;
+        if (j <= P) {
+          if constexpr (j > 1) {
+            const int a0 = (f0 / j) & ~3;
+            if (active) a += stage[p.soff[j] + (t / j) * p.sw[j] + f / j - a0];
+          }
+          const bool hit = active && a > p.hi[j - 1];
+          const bool near = active && !hit && a >= p.lo[j - 1];
+          const unsigned hm = __ballot_sync(0xffffffffu, hit);
+          if (hm) warp_emit(eb, warp, wcount, p, hm, j - 1, row, f, a);
+          const unsigned nm = __ballot_sync(0xffffffffu, near);
+          if (nm) warp_recheck(p, nm, j - 1, row, f);
         }
-        const bool hit = active && a > p.hi[j - 1];
-        const bool near = active && !hit && a >= p.lo[j - 1];
-        const unsigned hm = __ballot_sync(0xffffffffu, hit);
-        if (hm) warp_emit(eb, warp, wcount, p, hm, j - 1, row, f, a);
-        const unsigned nm = __ballot_sync(0xffffffffu, near);
-        if (nm) warp_recheck(p, nm, j - 1, row, f);
-      }
-    });
+      });
+    }
   }
   warp_flush(eb, warp, wcount, p);
 
   // ---- per-plane hit counts of the CTA
   __syncthreads();
   if (threadIdx.x < P && eb.pc[threadIdx.x]) atomicAdd(p.cand_count + threadIdx.x, eb.pc[threadIdx.x]);
+  (void)nwarps;
 }
 
 // One warp per recheck entry: HP_j of the cell in FP64 from the spectrum and
@@ -501,8 +562,9 @@ static cudaError_t launch_hsum_t(const HsumParams &p, cudaStream_t s) {
   const int smem = hsum_smem_bytes(p);
   cudaError_t e = cudaFuncSetAttribute(hsum_kernel<MAXP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
+  const int groups = (p.half + 1 + 3) / 4;  // warps: 4 templates each
   dim3 grid((p.n_bins + kHsBins - 1) / kHsBins, 2);
-  hsum_kernel<MAXP><<<grid, kHsThreads, smem, s>>>(p);
+  hsum_kernel<MAXP><<<grid, 32 * groups, smem, s>>>(p);
   return cudaGetLastError();
 }
 
