@@ -253,9 +253,10 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   }
   int off = 0;
   unsigned bytes = 0;
-  const int groups = (H + 1 + 3) / 4;  // the kernel's warps own |t| = 4w .. 4w+3
+  // the kernel's consumer warps (11, or 16 beyond 87 templates) own |t| = 4w .. 4w+3
+  const int nw = (H + 1 + 3) / 4 <= 11 ? 11 : 16;
   for (int j = 2; j <= P; ++j) {
-    p.srows[j] = (4 * groups - 1) / j + 2;  // + one spare row for the 2 x 2 windows
+    p.srows[j] = (4 * nw - 1) / j + 2;  // + one spare row for the 2 x 2 windows
     p.sw[j] = ((kHsBins - 1) / j + 6 + 3) & ~3;  // + 2x2-window spare column
     p.soff[j] = off;
     off += p.srows[j] * p.sw[j];
@@ -274,6 +275,8 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlStatus);
   p.timeout_ns = 2000000000LL;  // 2 s
 
+  if (hsum_smem_bytes(p) > 227 * 1024)
+    return fail(h, FDAS_ERR_UNSUPPORTED, "harmonic summing staging exceeds shared memory (too many templates x planes)");
   CK(h, cudaMemsetAsync(S.d_ctrl, 0, sizeof(unsigned) * kCtrlWords, S.stream));
   CK(h, launch_hsum(p, S.stream));
   if (recheck) {

@@ -137,219 +137,268 @@ __device__ __forceinline__ void warp_recheck(const HsumParams &p, unsigned nm, i
   }
 }
 
-// One CTA per (256-bin block, sign half), one warp per group of 4 templates:
-// warp w owns |t| = 4w + k (k < 4), lane l the bins f0 + 128 i + 4 l + e
-// (i < 2, e < 4), so every thread holds a 4 x 4 tile of cells aligned to 4 in
-// both directions.  For planes j >= 2 the rows trunc(t/j) and bins
-// [f0/j, (f0+255)/j] of the half are staged in shared memory by TMA bulk
-// copies (one per plane and row, 16-byte aligned); plane 1 is read from global
-// memory with 128-bit loads.  With the tile aligned to 4, planes 2, 4 and 8
-// map the 4 x 4 tile onto 2 x 2, 1 x 1 and 1 x 1 staged values at
-// compile-time offsets; planes 3, 5, 6, 7 onto a 2 x 2 window whose split
-// points are computed once per thread.
+// Persistent harmonic summing.  Work item = (256-bin block, sign half).  A
+// CTA has NW consumer warps -- warp w owns templates |t| = 4w + k (k < 4), lane
+// l the bins f0 + 128 i + 4 l + e (i < 2, e < 4), i.e. a 4 x 4 tile of cells
+// aligned to 4 in both directions -- and one producer warp that moves each
+// item's data into shared memory with TMA bulk copies (cp.async.bulk, one per
+// row): the 4 NW plane-1 rows [f0, f0+256) and, for planes j >= 2, the rows
+// trunc(t/j) over bins [f0/j, (f0+255)/j] (start rounded down to 16 bytes).
+// Two buffers: while the consumers work on item n the producer fills item
+// n+1 (full / empty mbarriers; every wait is bounded by %globaltimer).
+//
+// With the tile aligned to 4, planes 2, 4 and 8 map the 16 cells onto 2 x 2,
+// 1 and 1 staged values at compile-time offsets; planes 3, 5, 6, 7 onto a
+// 2 x 2 window whose split points are computed once per item.
 //
 // HP_1 = FOP[t][f], HP_j = HP_{j-1} + FOP[trunc(t/j)][f/j] accumulated in FP32
 // in this order -- hsum.py:95-120 / hms_baseline.cl.mako:55-84 -- so the
 // values match hsum.py bit for bit for the same FOP.  A cell is a candidate of
 // plane j if HP_j > thr_j (strict, hsum.py:134 / detect.cl.mako:185).  The fast
-// path only records, per thread, whether any cell reached the lower edge of a
-// threshold band; such warps re-walk their cells warp-synchronously and emit
-// through ballots.
-struct HsGeom {
-  const float *stage;
-  int f0, w, lane;
+// path keeps one flag per thread and sub-block (max over the 16 cells per
+// plane against the lower edge of the plane's band); flagged warps re-walk
+// their cells warp-synchronously and emit through ballots.
+struct HsItem {
+  int f0, sgn, tlo;
 };
 
-// value of plane j (>= 2) for cell (k, e) of this thread's tile, from the staged rows
+__device__ __forceinline__ HsItem hs_item(const HsumParams &p, int it) {
+  // items enumerate (block, half) over the enabled halves
+  const bool neg = p.tlo[0] <= p.half, pos = p.tlo[1] <= p.half;
+  int blk, halfsel;
+  if (neg && pos) { blk = it >> 1; halfsel = it & 1; }
+  else { blk = it; halfsel = pos ? 1 : 0; }
+  return HsItem{blk * kHsBins, halfsel ? 1 : -1, p.tlo[halfsel]};
+}
+
+__device__ __forceinline__ int hs_n_items(const HsumParams &p) {
+  const int nb = (p.n_bins + kHsBins - 1) / kHsBins;
+  return nb * ((p.tlo[0] <= p.half) + (p.tlo[1] <= p.half));
+}
+
 template <int J>
 struct PlaneWindow {
   float v00, v01, v10, v11;
   int kstar, estar;
-  __device__ __forceinline__ void load(const HsumParams &p, const HsGeom &g, int F) {
-    const int a0 = (g.f0 / J) & ~3;
-    const float *blk = g.stage + p.soff[J];
+  __device__ __forceinline__ void load(const float *stage, const HsumParams &p, int f0, int t0, int F) {
+    const int a0 = (f0 / J) & ~3;
     const int sw = p.sw[J];
-    const int t0 = 4 * g.w;
     const int rb = t0 / J;
     kstar = J - (t0 - rb * J);     // first k with trunc((t0+k)/J) = rb + 1
     const int bb = F / J;
     estar = J - (F - bb * J);      // first e with (F+e)/J = bb + 1
-    const float *r0 = blk + rb * sw + (bb - a0);
+    const float *r0 = stage + p.soff[J] + rb * sw + (bb - a0);
     v00 = r0[0];
     v01 = r0[1];
     v10 = r0[sw];
     v11 = r0[sw + 1];
   }
-  __device__ __forceinline__ float at(int k, int e) const {
-    const float c0 = e < estar ? v00 : v01;
-    const float c1 = e < estar ? v10 : v11;
-    return k < kstar ? c0 : c1;
-  }
 };
 
-template <int MAXP>
-__global__ void __launch_bounds__(512) hsum_kernel(HsumParams p) {
-  extern __shared__ __align__(128) float hs_smem[];
-  uint64_t *bar = reinterpret_cast<uint64_t *>(hs_smem);
-  float *stage = hs_smem + 4;
-  EmitBuf &eb = *reinterpret_cast<EmitBuf *>(hs_smem + 4 + ((p.smem_floats + 3) & ~3));
-  const int halfsel = blockIdx.y;
-  const int sgn = halfsel ? 1 : -1;
-  const int tlo = p.tlo[halfsel];
-  const int H = p.half;
-  if (tlo > H) return;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nwarps = blockDim.x >> 5;
-  const int f0 = blockIdx.x * kHsBins;
-  const int P = p.n_planes;
-  const bool staged = p.stage_bytes > 0;
+__device__ __forceinline__ float max16(const float (&a)[4][4]) {
+  float m0 = fmaxf(fmaxf(a[0][0], a[0][1]), fmaxf(a[0][2], a[0][3]));
+  float m1 = fmaxf(fmaxf(a[1][0], a[1][1]), fmaxf(a[1][2], a[1][3]));
+  float m2 = fmaxf(fmaxf(a[2][0], a[2][1]), fmaxf(a[2][2], a[2][3]));
+  float m3 = fmaxf(fmaxf(a[3][0], a[3][1]), fmaxf(a[3][2], a[3][3]));
+  return fmaxf(fmaxf(m0, m1), fmaxf(m2, m3));
+}
 
-  if (threadIdx.x == 0 && staged) {
-    mbar_init(bar, 1);
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait_parity(uint64_t *bar, uint32_t parity, long long timeout_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity))
+    if ((long long)(globaltimer_ns() - t0) > timeout_ns) return false;
+  return true;
+}
+
+template <int MAXP, int NW>
+__global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(HsumParams p) {
+  extern __shared__ __align__(128) float hs_smem[];
+  uint64_t *full = reinterpret_cast<uint64_t *>(hs_smem);       // [2]
+  uint64_t *empty = full + 2;                                     // [2]
+  constexpr int kRows1 = 4 * NW;
+  const int buf_floats = kRows1 * kHsBins + ((p.smem_floats + 3) & ~3);
+  float *bufs = hs_smem + 16;
+  EmitBuf &eb = *reinterpret_cast<EmitBuf *>(bufs + 2 * buf_floats);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int H = p.half;
+  const int P = p.n_planes;
+  const int n_items = hs_n_items(p);
+
+  if (threadIdx.x == 0) {
+    mbar_init(full, 1);
+    mbar_init(full + 1, 1);
+    mbar_init(empty, NW);
+    mbar_init(empty + 1, NW);
     fence_mbar_init();
   }
   if (threadIdx.x < kMaxPlanes) eb.pc[threadIdx.x] = 0;
   __syncthreads();
-  if (staged && warp == 0) {
-    if (lane == 0) mbar_arrive_expect_tx(bar, p.stage_bytes);
-    __syncwarp();
-    for (int j = 2; j <= P; ++j) {
-      const int a0 = (f0 / j) & ~3;
-      const int w = p.sw[j];
-      for (int r = lane; r < p.srows[j]; r += 32) {
-        // rows past |t| = H only feed cells that are masked out; copy row H instead
-        const float *src = p.fop + (long long)(H + sgn * min(r, H)) * p.stride + a0;
-        bulk_g2s(stage + p.soff[j] + r * w, src, (uint32_t)w * 4u, bar);
+
+  if (warp == NW) {
+    // ------------------------------------------------------------ producer
+    int n = 0;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x, ++n) {
+      const int b = n & 1, k = n >> 1;
+      if (k >= 1 && !mbar_wait_parity(empty + b, (k - 1) & 1, p.timeout_ns)) {
+        if (lane == 0) atomicOr(p.status, kStatusHsumTimeout);
+        break;
+      }
+      const HsItem item = hs_item(p, it);
+      float *rows1 = bufs + b * buf_floats;
+      float *stage = rows1 + kRows1 * kHsBins;
+      if (lane == 0) mbar_arrive_expect_tx(full + b, p.stage_bytes + (unsigned)(kRows1 * kHsBins * 4));
+      __syncwarp();
+      for (int r = lane; r < kRows1; r += 32) {
+        const float *src = p.fop + (long long)(H + item.sgn * min(r, H)) * p.stride + item.f0;
+        bulk_g2s(rows1 + r * kHsBins, src, kHsBins * 4u, full + b);
+      }
+      for (int j = 2; j <= P; ++j) {
+        const int a0 = (item.f0 / j) & ~3;
+        const int w = p.sw[j];
+        for (int r = lane; r < p.srows[j]; r += 32) {
+          // rows past |t| = H only feed masked cells; copy row H instead
+          const float *src = p.fop + (long long)(H + item.sgn * min(r, H)) * p.stride + a0;
+          bulk_g2s(stage + p.soff[j] + r * w, src, (uint32_t)w * 4u, full + b);
+        }
       }
     }
-  }
-
-  // rows of this warp: |t| = 4 warp + k; invalid ones (|t| > H or < tlo) get -inf
-  const int t0 = 4 * warp;
-  bool rowok[4];
+    // drain: wait (bounded) until the consumers released every buffer in use
+    const int used = n;
+    for (int m = used - 2; m < used; ++m)
+      if (m >= 0) mbar_wait_parity(empty + (m & 1), (m >> 1) & 1, p.timeout_ns);
+  } else {
+    // ------------------------------------------------------------ consumers
+    const int t0 = 4 * warp;
+    unsigned wcount = 0;
+    int n = 0;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x, ++n) {
+      const int b = n & 1, k = n >> 1;
+      if (!mbar_wait_parity(full + b, k & 1, p.timeout_ns)) {
+        if (lane == 0) atomicOr(p.status, kStatusHsumTimeout);
+        break;
+      }
+      const HsItem item = hs_item(p, it);
+      const int f0 = item.f0;
+      const float *rows1 = bufs + b * buf_floats;
+      const float *stage = rows1 + kRows1 * kHsBins;
+      bool rowok[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) rowok[k] = (t0 + k <= H) && (t0 + k >= tlo);
-
-  // plane 1 for both bin sub-blocks (loads in flight while the staging lands)
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    const int F = f0 + 128 * i + 4 * lane;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      float4 q = make_float4(-CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F);
-      if (rowok[k]) q = __ldg(reinterpret_cast<const float4 *>(p.fop + (long long)(H + sgn * (t0 + k)) * p.stride + F));
-      acc[i][k][0] = (F + 0 < p.n_bins) ? q.x : -CUDART_INF_F;
-      acc[i][k][1] = (F + 1 < p.n_bins) ? q.y : -CUDART_INF_F;
-      acc[i][k][2] = (F + 2 < p.n_bins) ? q.z : -CUDART_INF_F;
-      acc[i][k][3] = (F + 3 < p.n_bins) ? q.w : -CUDART_INF_F;
-    }
-  }
-  bool flag[2] = {false, false};
-  {
-    const float tr = p.trig[0];
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) flag[i] |= acc[i][k][e] >= tr;
-  }
-
-  // the timeout decision is made uniform over the CTA before any warp vote
-  bool ok = true;
-  if (staged) ok = __syncthreads_and(mbar_wait_bounded(bar, p.timeout_ns)) != 0;
-  if (!ok) {
-    if (threadIdx.x == 0) atomicOr(p.status, kStatusHsumTimeout);
-    mbar_wait_bounded(bar, p.timeout_ns);  // let copies in flight land (bounded)
-    return;
-  }
-  const HsGeom g{stage, f0, warp, lane};
-
-  // ---- fast path: planes 2..P, compile-time plane index
-  hs_sfor<MAXP - 1>([&](auto JJ) {
-    constexpr int j = decltype(JJ)::value + 2;
-    if (j <= P) {
-      const float tr = p.trig[j - 1];
+      for (int kk = 0; kk < 4; ++kk) rowok[kk] = (t0 + kk <= H) && (t0 + kk >= item.tlo);
+      const bool tail = f0 + kHsBins > p.n_bins;
+      unsigned flags = 0;
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
-        const int F = f0 + 128 * i + 4 * lane;
-        if constexpr (j == 2 || j == 4 || j == 8) {
-          const int a0 = (f0 / j) & ~3;
-          const float *blk = stage + p.soff[j] + (F / j - a0);
-          const int sw = p.sw[j];
-          if constexpr (j == 2) {
-            const float2 r0 = *reinterpret_cast<const float2 *>(blk + (t0 / 2) * sw);
-            const float2 r1 = *reinterpret_cast<const float2 *>(blk + (t0 / 2 + 1) * sw);
+        const int Fl = 128 * i + 4 * lane;   // bin within the block
+        const int F = f0 + Fl;
+        float acc[4][4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const float2 r = k < 2 ? r0 : r1;
-              acc[i][k][0] += r.x; acc[i][k][1] += r.x; acc[i][k][2] += r.y; acc[i][k][3] += r.y;
+        for (int kk = 0; kk < 4; ++kk) {
+          const float4 q = *reinterpret_cast<const float4 *>(rows1 + (t0 + kk) * kHsBins + Fl);
+          acc[kk][0] = q.x; acc[kk][1] = q.y; acc[kk][2] = q.z; acc[kk][3] = q.w;
+          if (!rowok[kk]) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = -CUDART_INF_F;
+        }
+        if (tail) {
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
+        }
+        bool flag = max16(acc) >= p.trig[0];
+        hs_sfor<MAXP - 1>([&](auto JJ) {
+          constexpr int j = decltype(JJ)::value + 2;
+          if (j <= P) {
+            if constexpr (j == 2 || j == 4 || j == 8) {
+              const int a0 = (f0 / j) & ~3;
+              const float *blk = stage + p.soff[j] + (F / j - a0);
+              const int sw = p.sw[j];
+              if constexpr (j == 2) {
+                const float2 r0 = *reinterpret_cast<const float2 *>(blk + (t0 / 2) * sw);
+                const float2 r1 = *reinterpret_cast<const float2 *>(blk + (t0 / 2 + 1) * sw);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                  const float2 r = kk < 2 ? r0 : r1;
+                  acc[kk][0] += r.x; acc[kk][1] += r.x; acc[kk][2] += r.y; acc[kk][3] += r.y;
+                }
+              } else {
+                const float v = blk[(t0 / j) * sw];
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+                  for (int e = 0; e < 4; ++e) acc[kk][e] += v;
+              }
+            } else {
+              PlaneWindow<j> win;
+              win.load(stage, p, f0, t0, F);
+              float c0[4], c1[4];
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                c0[e] = e < win.estar ? win.v00 : win.v01;
+                c1[e] = e < win.estar ? win.v10 : win.v11;
+              }
+#pragma unroll
+              for (int kk = 0; kk < 4; ++kk) {
+                if (kk < win.kstar) {  // warp-uniform
+#pragma unroll
+                  for (int e = 0; e < 4; ++e) acc[kk][e] += c0[e];
+                } else {
+#pragma unroll
+                  for (int e = 0; e < 4; ++e) acc[kk][e] += c1[e];
+                }
+              }
             }
-          } else {
-            const float v = blk[(t0 / j) * sw];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-#pragma unroll
-              for (int e = 0; e < 4; ++e) acc[i][k][e] += v;
+            flag |= max16(acc) >= p.trig[j - 1];
           }
-        } else {
-          PlaneWindow<j> win;
-          win.load(p, g, F);
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[i][k][e] += win.at(k, e);
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-#pragma unroll
-          for (int e = 0; e < 4; ++e) flag[i] |= acc[i][k][e] >= tr;
+        });
+        if (flag) flags |= 1u << i;
       }
-    }
-  });
 
-  // ---- slow path (rare): warps with a flagged lane re-walk their cells in the
-  // same order; every lane recomputes its own cell and emission goes through
-  // warp ballots into the warp's record buffer
-  unsigned wcount = 0;
-  const unsigned flags = (flag[0] ? 1u : 0u) | (flag[1] ? 2u : 0u);
+      // ---- slow path (rare): re-walk the flagged sub-blocks of the warp
 #pragma unroll 1
-  for (int i = 0; i < 2; ++i) {
-    const bool fl = (flags >> i) & 1u;
-    if (!__any_sync(0xffffffffu, fl)) continue;
-    const int F = f0 + 128 * i + 4 * lane;
+      for (int i = 0; i < 2; ++i) {
+        const bool fl = (flags >> i) & 1u;
+        if (!__any_sync(0xffffffffu, fl)) continue;
+        const int Fl = 128 * i + 4 * lane;
+        const int F = f0 + Fl;
 #pragma unroll 1
-    for (int c = 0; c < 16; ++c) {
-      const int k = c >> 2, e = c & 3;
-      const int t = t0 + k;
-      const int f = F + e;
-      const bool active = fl && t <= H && t >= tlo && f < p.n_bins;
-      const int row = H + sgn * t;
-      float a = active ? p.fop[(long long)row * p.stride + f] : 0.f;
-      hs_sfor<MAXP>([&](auto JJ) {
-        constexpr int j = decltype(JJ)::value + 1;
-        if (j <= P) {
-          if constexpr (j > 1) {
-            const int a0 = (f0 / j) & ~3;
-            if (active) a += stage[p.soff[j] + (t / j) * p.sw[j] + f / j - a0];
-          }
-          const bool hit = active && a > p.hi[j - 1];
-          const bool near = active && !hit && a >= p.lo[j - 1];
-          const unsigned hm = __ballot_sync(0xffffffffu, hit);
-          if (hm) warp_emit(eb, warp, wcount, p, hm, j - 1, row, f, a);
-          const unsigned nm = __ballot_sync(0xffffffffu, near);
-          if (nm) warp_recheck(p, nm, j - 1, row, f);
+        for (int c = 0; c < 16; ++c) {
+          const int kk = c >> 2, e = c & 3;
+          const int t = t0 + kk;
+          const int f = F + e;
+          const bool active = fl && t <= H && t >= item.tlo && f < p.n_bins;
+          const int row = H + item.sgn * t;
+          float a = active ? rows1[t * kHsBins + Fl + e] : 0.f;
+          hs_sfor<MAXP>([&](auto JJ) {
+            constexpr int j = decltype(JJ)::value + 1;
+            if (j <= P) {
+              if constexpr (j > 1) {
+                const int a0 = (f0 / j) & ~3;
+                if (active) a += stage[p.soff[j] + (t / j) * p.sw[j] + f / j - a0];
+              }
+              const bool hit = active && a > p.hi[j - 1];
+              const bool near = active && !hit && a >= p.lo[j - 1];
+              const unsigned hm = __ballot_sync(0xffffffffu, hit);
+              if (hm) warp_emit(eb, warp, wcount, p, hm, j - 1, row, f, a);
+              const unsigned nm = __ballot_sync(0xffffffffu, near);
+              if (nm) warp_recheck(p, nm, j - 1, row, f);
+            }
+          });
         }
-      });
+      }
+      // release the buffer to the producer
+      __syncwarp();
+      if (lane == 0) mbar_arrive(empty + b);
     }
+    warp_flush(eb, warp, wcount, p);
   }
-  warp_flush(eb, warp, wcount, p);
 
   // ---- per-plane hit counts of the CTA
   __syncthreads();
   if (threadIdx.x < P && eb.pc[threadIdx.x]) atomicAdd(p.cand_count + threadIdx.x, eb.pc[threadIdx.x]);
-  (void)nwarps;
 }
 
 // One warp per recheck entry: HP_j of the cell in FP64 from the spectrum and
@@ -370,7 +419,9 @@ __global__ void __launch_bounds__(256) recheck_kernel(RecheckParams p) {
       const int len = p.tap_len[r];
       const double2 *h = p.taps + (long long)r * p.tap_pitch;
       double re = 0.0, im = 0.0;
-      for (int q = lane; q < len && q <= g; q += 32) {
+      const int qn = min(len, g + 1);
+#pragma unroll 4
+      for (int q = lane; q < qn; q += 32) {
         const float2 x = p.input[g - q];
         const double2 c = h[q];
         re += (double)x.x * c.x - (double)x.y * c.y;
@@ -413,16 +464,21 @@ __global__ void __launch_bounds__(256) select_hist_kernel(SelectParams p) {
   const unsigned n = stored_records(p);
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int plane = (int)(p.cand_key[i] >> 48);
-    if (p.cand_count[plane] > (unsigned)p.per_plane)
-      atomicAdd(p.hist + (size_t)plane * kSelBuckets + (float_key(p.cand_pwr[i]) >> 16), 1u);
+    if (p.cand_count[plane] > (unsigned)p.per_plane) {
+      const unsigned idx = (unsigned)plane * kSelBuckets + (float_key(p.cand_pwr[i]) >> 16);
+      // records of similar power share buckets: one atomic per distinct bucket of the warp
+      const unsigned peers = __match_any_sync(__activemask(), idx);
+      if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(p.hist + idx, (unsigned)__popc(peers));
+    }
   }
 }
 
-// One CTA (1024 threads) per plane: thread t owns buckets
-// [kSelBuckets - 64 (t+1), kSelBuckets - 64 t), i.e. thread 0 the strongest.
+// One CTA (32 warps) per plane.  Warp w owns the 2048 buckets
+// [kSelBuckets - 2048 (w+1), kSelBuckets - 2048 w) (warp 0 the strongest);
+// all reads are coalesced.  The warp whose segment holds the K-th strongest
+// record scans it 32 buckets at a time from the top.
 __global__ void __launch_bounds__(1024) select_threshold_kernel(SelectParams p) {
-  __shared__ unsigned part[1024];
-  __shared__ unsigned found;
+  __shared__ unsigned seg[32];
   const int plane = blockIdx.x;
   unsigned *h = p.hist + (size_t)plane * kSelBuckets;
   const unsigned K = (unsigned)p.per_plane;
@@ -430,35 +486,54 @@ __global__ void __launch_bounds__(1024) select_threshold_kernel(SelectParams p) 
     if (threadIdx.x == 0) p.sel_lo[plane] = 0u;
     return;
   }
-  const int t = threadIdx.x;
-  const int hi_b = kSelBuckets - 64 * t;  // exclusive
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int kSeg = kSelBuckets / 32;
+  const int top = kSelBuckets - kSeg * warp;  // exclusive
   unsigned local = 0;
-  for (int b = hi_b - 64; b < hi_b; ++b) local += h[b];
-  part[t] = local;
-  if (t == 0) found = 0u;
+  for (int b = top - 1 - lane; b >= top - kSeg; b -= 32) local += h[b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if (lane == 0) seg[warp] = local;
   __syncthreads();
-  // inclusive scan over threads (strongest first)
-  for (int o = 1; o < 1024; o <<= 1) {
-    const unsigned v = t >= o ? part[t - o] : 0u;
-    __syncthreads();
-    part[t] += v;
-    __syncthreads();
-  }
-  const unsigned before = t ? part[t - 1] : 0u;
-  if (before < K && part[t] >= K) {
-    unsigned c = before;
-    int b = hi_b - 1;
-    for (; b >= hi_b - 64; --b) {
-      c += h[b];
-      if (c >= K) break;
+  if (warp == 0) {
+    // inclusive scan of the segment totals, strongest first
+    unsigned v = seg[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
     }
-    p.sel_lo[plane] = (unsigned)b << 16;
-    found = 1u;
+    const unsigned before = __shfl_up_sync(0xffffffffu, v, 1);
+    seg[lane] = lane ? before : 0u;  // exclusive prefix
+    const unsigned crossing = __ballot_sync(0xffffffffu, v >= K);
+    if (lane == 0 && !crossing) p.sel_lo[plane] = 0u;  // fewer stored than K (overflow): take all
   }
   __syncthreads();
-  if (t == 0 && !found) p.sel_lo[plane] = 0u;  // fewer stored than K (overflow): take all
+  const unsigned before = seg[warp];
+  const unsigned after = (warp < 31) ? seg[warp + 1] : 0xffffffffu;
+  if (before < K && (warp == 31 || after >= K)) {
+    // this warp's segment holds the crossing
+    unsigned c = before;
+    for (int chunk = top; chunk > top - kSeg; chunk -= 32) {
+      const int b = chunk - 1 - lane;  // lane 0 = strongest of the chunk
+      unsigned v = h[b];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+      }
+      const unsigned hit = __ballot_sync(0xffffffffu, c + v >= K);
+      if (hit) {
+        const int l = __ffs(hit) - 1;
+        if (lane == 0) p.sel_lo[plane] = (unsigned)(chunk - 1 - l) << 16;
+        break;
+      }
+      c += __shfl_sync(0xffffffffu, v, 31);
+    }
+  }
+  __syncthreads();
   // leave the histogram zeroed for the next search
-  for (int b = hi_b - 64; b < hi_b; ++b)
+  for (int b = top - 1 - lane; b >= top - kSeg; b -= 32)
     if (h[b]) h[b] = 0u;
 }
 
@@ -553,25 +628,39 @@ __global__ void __launch_bounds__(1024) select_finalize_kernel(SelectParams p) {
 }
 
 // ----------------------------------------------------------------- launchers
+static int hs_warps(const HsumParams &p) { return (p.half + 1 + 3) / 4; }
+
 int hsum_smem_bytes(const HsumParams &p) {
-  return 16 + ((p.smem_floats + 3) & ~3) * 4 + (int)sizeof(EmitBuf);
+  const int nw = hs_warps(p) <= 11 ? 11 : 16;
+  const int buf_floats = 4 * nw * kHsBins + ((p.smem_floats + 3) & ~3);
+  return 16 * 4 + 2 * buf_floats * 4 + (int)sizeof(EmitBuf);
 }
 
-template <int MAXP>
+template <int MAXP, int NW>
 static cudaError_t launch_hsum_t(const HsumParams &p, cudaStream_t s) {
   const int smem = hsum_smem_bytes(p);
-  cudaError_t e = cudaFuncSetAttribute(hsum_kernel<MAXP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = cudaFuncSetAttribute(hsum_kernel<MAXP, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  const int groups = (p.half + 1 + 3) / 4;  // warps: 4 templates each
-  dim3 grid((p.n_bins + kHsBins - 1) / kHsBins, 2);
-  hsum_kernel<MAXP><<<grid, 32 * groups, smem, s>>>(p);
+  static int n_sm = 0;
+  if (!n_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (n_sm <= 0) n_sm = 1;
+  }
+  const int nb = (p.n_bins + kHsBins - 1) / kHsBins;
+  const int items = nb * 2;
+  hsum_kernel<MAXP, NW><<<items < n_sm ? items : n_sm, 32 * (NW + 1), smem, s>>>(p);
   return cudaGetLastError();
 }
 
 cudaError_t launch_hsum(const HsumParams &p, cudaStream_t s) {
-  if (p.n_planes <= 4) return launch_hsum_t<4>(p, s);
-  if (p.n_planes <= 8) return launch_hsum_t<8>(p, s);
-  return launch_hsum_t<16>(p, s);
+  // warps own 4 templates each: 11 warps cover up to 87 templates, 16 up to 127
+  if (hs_warps(p) <= 11) {
+    if (p.n_planes <= 8) return launch_hsum_t<8, 11>(p, s);
+    return launch_hsum_t<16, 11>(p, s);
+  }
+  return launch_hsum_t<16, 16>(p, s);
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
