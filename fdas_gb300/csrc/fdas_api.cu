@@ -32,7 +32,8 @@ constexpr int kCtrlTotal = 2;                       // records appended
 constexpr int kCtrlCount = 3;                       // + plane: hits per plane
 constexpr int kCtrlSelCount = kCtrlCount + kMaxPlanes;
 constexpr int kCtrlSelLo = kCtrlSelCount + kMaxPlanes;
-constexpr int kCtrlWords = kCtrlSelLo + kMaxPlanes;
+constexpr int kCtrlItems = kCtrlSelLo + kMaxPlanes;  // harmonic-summing work counter
+constexpr int kCtrlWords = kCtrlItems + 1;
 constexpr uint32_t kDefaultCapacity = 1u << 22;     // candidate records per buffer set
 constexpr uint32_t kMaxCapacity = 1u << 27;
 constexpr int kRecheckCap = 65536;
@@ -58,6 +59,7 @@ struct BufferSet {
   uint32_t *d_cloc = nullptr;
   float *d_cpwr = nullptr;
   cudaEvent_t ev[kNumEvents] = {};
+  HsumMaps maps;  // TMA descriptors of this set's FOP
   bool have_templates = false;
   bool have_taps = false;
   bool have_input = false;
@@ -160,6 +162,64 @@ void rows_of(const fdas_handle *h, fdas_fop_part w, int *row_begin, int *n_rows)
   else { *row_begin = 0; *n_rows = h->T; }
 }
 
+// ------------------------------------------------- harmonic-summing geometry
+// Box shapes of the per-item staging (see hsum_kernel): plane 1 is 128 bins x
+// 4 NW rows, plane j >= 2 covers bins [(f0/j) & ~3, ...) of the rows
+// trunc(|t|/j), |t| < 4 NW, with one spare row and column for the 2 x 2 windows.
+void hsum_geometry(const fdas_handle *h, HsumParams &p) {
+  const int nw = hsum_warps(h->H);
+  p.bw[1] = kHsBins;
+  p.bh[1] = 4 * nw;
+  int off = 0;
+  p.soff[1] = off;
+  off += p.bw[1] * p.bh[1];
+  unsigned bytes = (unsigned)(p.bw[1] * p.bh[1] * 4);
+  for (int j = 2; j <= h->P; ++j) {
+    p.bw[j] = ((kHsBins - 1) / j + 6 + 3) & ~3;
+    p.bh[j] = (4 * nw - 1) / j + 2;
+    off = (off + 31) & ~31;  // 128-byte aligned TMA destinations
+    p.soff[j] = off;
+    off += p.bw[j] * p.bh[j];
+    bytes += (unsigned)(p.bw[j] * p.bh[j] * 4);
+  }
+  p.stage_floats = (off + 255) & ~255;  // 1 KB aligned stages
+  p.stage_bytes = bytes;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+fdas_status make_hsum_maps(fdas_handle *h, BufferSet &S) {
+  static EncodeTiledFn encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+      return fail(h, FDAS_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    encode = reinterpret_cast<EncodeTiledFn>(fn);
+  }
+  HsumParams g{};
+  hsum_geometry(h, g);
+  std::memset(&S.maps, 0, sizeof(S.maps));
+  for (int j = 1; j <= h->P; ++j) {
+    const cuuint64_t dims[2] = {(cuuint64_t)h->stride, (cuuint64_t)h->T};
+    const cuuint64_t strides[1] = {(cuuint64_t)h->stride * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)g.bw[j], (cuuint32_t)g.bh[j]};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(&S.maps.map[j], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, S.d_fop, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      char msg[128];
+      snprintf(msg, sizeof(msg), "cuTensorMapEncodeTiled failed (%d) for plane %d", (int)r, j);
+      return fail(h, FDAS_ERR_CUDA, msg);
+    }
+  }
+  return FDAS_OK;
+}
+
 // ---------------------------------------------------------------- stages
 fdas_status enqueue_input(fdas_handle *h, int ab, const fdas_complex *input, bool device_ptr) {
   BufferSet &S = h->set[ab];
@@ -253,17 +313,8 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   }
   int off = 0;
   unsigned bytes = 0;
-  // the kernel's consumer warps (11, or 16 beyond 87 templates) own |t| = 4w .. 4w+3
-  const int nw = (H + 1 + 3) / 4 <= 11 ? 11 : 16;
-  for (int j = 2; j <= P; ++j) {
-    p.srows[j] = (4 * nw - 1) / j + 2;  // + one spare row for the 2 x 2 windows
-    p.sw[j] = ((kHsBins - 1) / j + 6 + 3) & ~3;  // + 2x2-window spare column
-    p.soff[j] = off;
-    off += p.srows[j] * p.sw[j];
-    bytes += (unsigned)(p.srows[j] * p.sw[j] * 4);
-  }
-  p.smem_floats = off;
-  p.stage_bytes = bytes;
+  hsum_geometry(h, p);
+  p.item_counter = S.d_ctrl + kCtrlItems;
   p.cand_key = S.d_key;
   p.cand_pwr = S.d_pwr;
   p.cand_total = S.d_ctrl + kCtrlTotal;
@@ -278,7 +329,7 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   if (hsum_smem_bytes(p) > 227 * 1024)
     return fail(h, FDAS_ERR_UNSUPPORTED, "harmonic summing staging exceeds shared memory (too many templates x planes)");
   CK(h, cudaMemsetAsync(S.d_ctrl, 0, sizeof(unsigned) * kCtrlWords, S.stream));
-  CK(h, launch_hsum(p, S.stream));
+  CK(h, launch_hsum(p, S.maps, S.stream));
   if (recheck) {
     RecheckParams r{};
     r.input = S.cur_input;
@@ -527,6 +578,7 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
       return bail(FDAS_ERR_CUDA);
     }
     std::memset(S.h_ctrl, 0, sizeof(unsigned) * kCtrlWords);
+    if (make_hsum_maps(h, S) != FDAS_OK) return bail(FDAS_ERR_CUDA);
     for (auto &ev : S.ev) {
       if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
         cuda_fail(h, e, "cudaEventCreate", __FILE__, __LINE__);

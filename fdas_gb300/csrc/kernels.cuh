@@ -1,6 +1,7 @@
 // Kernel parameter blocks and launchers of the FDAS hot path.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -8,7 +9,7 @@ namespace fdas {
 
 constexpr int kTile = 2048;          // FFT / tile size (gen_info.h:33, 42)
 constexpr int kMaxPlanes = 16;       // harmonic planes supported by the kernels
-constexpr int kHsBins = 256;         // bins per harmonic-summing CTA
+constexpr int kHsBins = 128;         // bins per harmonic-summing work item
 constexpr int kSortCap = 8192;       // records one CTA sorts in shared memory
 constexpr int kEmitBuf = 1024;       // candidate records staged per harmonic-summing CTA
 constexpr int kSelBuckets = 65536;   // power buckets of the top-K selection (top 16 key bits)
@@ -67,11 +68,14 @@ struct HsumParams {
   float trig[kMaxPlanes]; // fast-path trigger: a cell needs a closer look if HP >= trig
   float hi[kMaxPlanes];   // candidate if HP > hi
   float lo[kMaxPlanes];   // recheck if lo <= HP <= hi (lo = +inf: never)
-  int sw[kMaxPlanes + 1];   // staged row width (floats) of plane j
-  int soff[kMaxPlanes + 1]; // offset (floats) of plane j's staging block
-  int srows[kMaxPlanes + 1];// rows staged for plane j
-  unsigned stage_bytes;   // total bytes moved by the bulk copies
-  int smem_floats;        // staging floats (after the 16-byte barrier slot)
+  // staging boxes: plane 1 is 128 bins x 4 NW rows; plane j >= 2 is bw[j] bins
+  // (from (f0/j) rounded down to 4) x bh[j] rows (trunc(t/j) of the half)
+  int bw[kMaxPlanes + 1];
+  int bh[kMaxPlanes + 1];
+  int soff[kMaxPlanes + 1]; // float offset of plane j's box in a stage (128-byte aligned)
+  int stage_floats;         // floats per pipeline stage
+  unsigned stage_bytes;     // bytes the TMA copies deliver per stage
+  unsigned *item_counter;   // dynamic work distribution
   unsigned long long *cand_key;  // [cap] records, any order
   float *cand_pwr;               // [cap]
   unsigned *cand_total;          // records appended (may exceed cap)
@@ -82,6 +86,11 @@ struct HsumParams {
   int rc_cap;
   int *status;
   long long timeout_ns;   // bound on every wait
+};
+
+// 2-D tensor maps of the FOP (rows x stride floats), one box shape per plane
+struct HsumMaps {
+  CUtensorMap map[kMaxPlanes + 1];
 };
 
 // ---- FP64 recheck of near-threshold cells
@@ -146,7 +155,9 @@ struct TapsParams {
 
 cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s);
 cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s);
-cudaError_t launch_hsum(const HsumParams &p, cudaStream_t s);
+cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s);
+// consumer warps of the harmonic-summing kernel for `half` (4 templates each)
+int hsum_warps(int half);
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s);
 cudaError_t launch_select(const SelectParams &p, cudaStream_t s);
 cudaError_t launch_spectra(const SpectraParams &p, cudaStream_t s);
@@ -154,5 +165,6 @@ cudaError_t launch_taps(const TapsParams &p, cudaStream_t s);
 
 // shared memory bytes needed by launch_hsum for a given plane geometry
 int hsum_smem_bytes(const HsumParams &p);
+constexpr int kStatusHsumSetup = 32;
 
 }  // namespace fdas

@@ -137,15 +137,16 @@ __device__ __forceinline__ void warp_recheck(const HsumParams &p, unsigned nm, i
   }
 }
 
-// Persistent harmonic summing.  Work item = (256-bin block, sign half).  A
-// CTA has NW consumer warps -- warp w owns templates |t| = 4w + k (k < 4), lane
-// l the bins f0 + 128 i + 4 l + e (i < 2, e < 4), i.e. a 4 x 4 tile of cells
-// aligned to 4 in both directions -- and one producer warp that moves each
-// item's data into shared memory with TMA bulk copies (cp.async.bulk, one per
-// row): the 4 NW plane-1 rows [f0, f0+256) and, for planes j >= 2, the rows
-// trunc(t/j) over bins [f0/j, (f0+255)/j] (start rounded down to 16 bytes).
-// Two buffers: while the consumers work on item n the producer fills item
-// n+1 (full / empty mbarriers; every wait is bounded by %globaltimer).
+// Persistent harmonic summing.  Work item = (128-bin block, sign half),
+// handed out dynamically through a global counter.  A CTA has NW consumer
+// warps -- warp w owns templates |t| = 4w + k (k < 4), lane l the bins
+// f0 + 4 l + e (e < 4), i.e. a 4 x 4 tile of cells aligned to 4 in both
+// directions -- and one producer warp.  For every item the producer issues one
+// 2-D TMA tensor copy per plane (cp.async.bulk.tensor.2d): plane 1 as 128 bins
+// x 4 NW rows, plane j >= 2 as the rows trunc(t/j) of the half over bins
+// [(f0/j) & ~3, ...); rows and bins outside the FOP are zero-filled by the
+// hardware (they only feed masked cells).  kHsStages stages deep: full /
+// empty mbarriers, every wait bounded by %globaltimer.
 //
 // With the tile aligned to 4, planes 2, 4 and 8 map the 16 cells onto 2 x 2,
 // 1 and 1 staged values at compile-time offsets; planes 3, 5, 6, 7 onto a
@@ -155,9 +156,9 @@ __device__ __forceinline__ void warp_recheck(const HsumParams &p, unsigned nm, i
 // in this order -- hsum.py:95-120 / hms_baseline.cl.mako:55-84 -- so the
 // values match hsum.py bit for bit for the same FOP.  A cell is a candidate of
 // plane j if HP_j > thr_j (strict, hsum.py:134 / detect.cl.mako:185).  The fast
-// path keeps one flag per thread and sub-block (max over the 16 cells per
-// plane against the lower edge of the plane's band); flagged warps re-walk
-// their cells warp-synchronously and emit through ballots.
+// path keeps one flag per thread (max over the 16 cells per plane against the
+// lower edge of the plane's band); flagged warps re-walk their cells
+// warp-synchronously and emit through ballots.
 struct HsItem {
   int f0, sgn, tlo;
 };
@@ -175,25 +176,6 @@ __device__ __forceinline__ int hs_n_items(const HsumParams &p) {
   const int nb = (p.n_bins + kHsBins - 1) / kHsBins;
   return nb * ((p.tlo[0] <= p.half) + (p.tlo[1] <= p.half));
 }
-
-template <int J>
-struct PlaneWindow {
-  float v00, v01, v10, v11;
-  int kstar, estar;
-  __device__ __forceinline__ void load(const float *stage, const HsumParams &p, int f0, int t0, int F) {
-    const int a0 = (f0 / J) & ~3;
-    const int sw = p.sw[J];
-    const int rb = t0 / J;
-    kstar = J - (t0 - rb * J);     // first k with trunc((t0+k)/J) = rb + 1
-    const int bb = F / J;
-    estar = J - (F - bb * J);      // first e with (F+e)/J = bb + 1
-    const float *r0 = stage + p.soff[J] + rb * sw + (bb - a0);
-    v00 = r0[0];
-    v01 = r0[1];
-    v10 = r0[sw];
-    v11 = r0[sw + 1];
-  }
-};
 
 __device__ __forceinline__ float max16(const float (&a)[4][4]) {
   float m0 = fmaxf(fmaxf(a[0][0], a[0][1]), fmaxf(a[0][2], a[0][3]));
@@ -213,26 +195,38 @@ __device__ __forceinline__ bool mbar_wait_parity(uint64_t *bar, uint32_t parity,
     if ((long long)(globaltimer_ns() - t0) > timeout_ns) return false;
   return true;
 }
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
 
-template <int MAXP, int NW>
-__global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(HsumParams p) {
-  extern __shared__ __align__(128) float hs_smem[];
-  uint64_t *full = reinterpret_cast<uint64_t *>(hs_smem);       // [2]
-  uint64_t *empty = full + 2;                                     // [2]
+// smem row of staged row r (r = |t| or trunc(|t|/j)) in a box of bh rows: the
+// boxes hold FOP rows in ascending order, i.e. reversed for the negative half
+__device__ __forceinline__ int srow(int r, int bh, int sgn) { return sgn > 0 ? r : bh - 1 - r; }
+
+template <int MAXP, int NW, int kHsStages>
+__global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_constant__ HsumParams p,
+                                                                 const __grid_constant__ HsumMaps m) {
+  extern __shared__ __align__(1024) float hs_smem[];
+  uint64_t *full = reinterpret_cast<uint64_t *>(hs_smem);  // [kHsStages]
+  uint64_t *empty = full + kHsStages;                        // [kHsStages]
+  int *item_id = reinterpret_cast<int *>(empty + kHsStages); // [kHsStages]
+  float *stages = hs_smem + 256;                             // 1 KB header
+  EmitBuf &eb = *reinterpret_cast<EmitBuf *>(stages + kHsStages * p.stage_floats);
   constexpr int kRows1 = 4 * NW;
-  const int buf_floats = kRows1 * kHsBins + ((p.smem_floats + 3) & ~3);
-  float *bufs = hs_smem + 16;
-  EmitBuf &eb = *reinterpret_cast<EmitBuf *>(bufs + 2 * buf_floats);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int H = p.half;
   const int P = p.n_planes;
   const int n_items = hs_n_items(p);
 
   if (threadIdx.x == 0) {
-    mbar_init(full, 1);
-    mbar_init(full + 1, 1);
-    mbar_init(empty, NW);
-    mbar_init(empty + 1, NW);
+    for (int s = 0; s < kHsStages; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, NW);
+    }
     fence_mbar_init();
   }
   if (threadIdx.x < kMaxPlanes) eb.pc[threadIdx.x] = 0;
@@ -240,144 +234,137 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(HsumParams p) {
 
   if (warp == NW) {
     // ------------------------------------------------------------ producer
-    int n = 0;
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x, ++n) {
-      const int b = n & 1, k = n >> 1;
-      if (k >= 1 && !mbar_wait_parity(empty + b, (k - 1) & 1, p.timeout_ns)) {
-        if (lane == 0) atomicOr(p.status, kStatusHsumTimeout);
-        break;
-      }
-      const HsItem item = hs_item(p, it);
-      float *rows1 = bufs + b * buf_floats;
-      float *stage = rows1 + kRows1 * kHsBins;
-      if (lane == 0) mbar_arrive_expect_tx(full + b, p.stage_bytes + (unsigned)(kRows1 * kHsBins * 4));
-      __syncwarp();
-      for (int r = lane; r < kRows1; r += 32) {
-        const float *src = p.fop + (long long)(H + item.sgn * min(r, H)) * p.stride + item.f0;
-        bulk_g2s(rows1 + r * kHsBins, src, kHsBins * 4u, full + b);
-      }
-      for (int j = 2; j <= P; ++j) {
-        const int a0 = (item.f0 / j) & ~3;
-        const int w = p.sw[j];
-        for (int r = lane; r < p.srows[j]; r += 32) {
-          // rows past |t| = H only feed masked cells; copy row H instead
-          const float *src = p.fop + (long long)(H + item.sgn * min(r, H)) * p.stride + a0;
-          bulk_g2s(stage + p.soff[j] + r * w, src, (uint32_t)w * 4u, full + b);
+    if (lane == 0) {
+      for (int s = 0;; ++s) {
+        const int st = s % kHsStages, use = s / kHsStages;
+        if (use >= 1 && !mbar_wait_parity(empty + st, (use - 1) & 1, p.timeout_ns)) {
+          atomicOr(p.status, kStatusHsumTimeout);
+          item_id[st] = -1;
+          mbar_arrive(full + st);
+          break;
+        }
+        const int it = (int)atomicAdd(p.item_counter, 1u);
+        if (it >= n_items) {
+          item_id[st] = -1;
+          mbar_arrive(full + st);  // plain arrival: the stage carries the stop mark
+          break;
+        }
+        item_id[st] = it;
+        const HsItem item = hs_item(p, it);
+        float *stage = stages + st * p.stage_floats;
+        mbar_arrive_expect_tx(full + st, p.stage_bytes);
+        tma_load_2d(stage + p.soff[1], &m.map[1], item.f0, item.sgn > 0 ? H : H - (kRows1 - 1), full + st);
+        for (int j = 2; j <= P; ++j) {
+          const int a0 = (item.f0 / j) & ~3;
+          tma_load_2d(stage + p.soff[j], &m.map[j], a0, item.sgn > 0 ? H : H - (p.bh[j] - 1), full + st);
         }
       }
     }
-    // drain: wait (bounded) until the consumers released every buffer in use
-    const int used = n;
-    for (int m = used - 2; m < used; ++m)
-      if (m >= 0) mbar_wait_parity(empty + (m & 1), (m >> 1) & 1, p.timeout_ns);
   } else {
     // ------------------------------------------------------------ consumers
     const int t0 = 4 * warp;
     unsigned wcount = 0;
-    int n = 0;
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x, ++n) {
-      const int b = n & 1, k = n >> 1;
-      if (!mbar_wait_parity(full + b, k & 1, p.timeout_ns)) {
+    for (int s = 0;; ++s) {
+      const int st = s % kHsStages, use = s / kHsStages;
+      if (!mbar_wait_parity(full + st, use & 1, p.timeout_ns)) {
         if (lane == 0) atomicOr(p.status, kStatusHsumTimeout);
         break;
       }
+      const int it = item_id[st];
+      if (it < 0) break;
       const HsItem item = hs_item(p, it);
-      const int f0 = item.f0;
-      const float *rows1 = bufs + b * buf_floats;
-      const float *stage = rows1 + kRows1 * kHsBins;
+      const int f0 = item.f0, sgn = item.sgn;
+      const float *stage = stages + st * p.stage_floats;
+      const int F = f0 + 4 * lane;
       bool rowok[4];
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk) rowok[kk] = (t0 + kk <= H) && (t0 + kk >= item.tlo);
-      const bool tail = f0 + kHsBins > p.n_bins;
-      unsigned flags = 0;
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int Fl = 128 * i + 4 * lane;   // bin within the block
-        const int F = f0 + Fl;
-        float acc[4][4];
+      float acc[4][4];
+      {
+        const float *r1 = stage + p.soff[1] + 4 * lane;
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) {
-          const float4 q = *reinterpret_cast<const float4 *>(rows1 + (t0 + kk) * kHsBins + Fl);
+          const float4 q = *reinterpret_cast<const float4 *>(r1 + srow(t0 + kk, kRows1, sgn) * kHsBins);
           acc[kk][0] = q.x; acc[kk][1] = q.y; acc[kk][2] = q.z; acc[kk][3] = q.w;
           if (!rowok[kk]) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = -CUDART_INF_F;
         }
-        if (tail) {
+      }
+      if (f0 + kHsBins > p.n_bins) {
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
+        for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-              if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
-        }
-        bool flag = max16(acc) >= p.trig[0];
-        hs_sfor<MAXP - 1>([&](auto JJ) {
-          constexpr int j = decltype(JJ)::value + 2;
-          if (j <= P) {
-            if constexpr (j == 2 || j == 4 || j == 8) {
-              const int a0 = (f0 / j) & ~3;
-              const float *blk = stage + p.soff[j] + (F / j - a0);
-              const int sw = p.sw[j];
-              if constexpr (j == 2) {
-                const float2 r0 = *reinterpret_cast<const float2 *>(blk + (t0 / 2) * sw);
-                const float2 r1 = *reinterpret_cast<const float2 *>(blk + (t0 / 2 + 1) * sw);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                  const float2 r = kk < 2 ? r0 : r1;
-                  acc[kk][0] += r.x; acc[kk][1] += r.x; acc[kk][2] += r.y; acc[kk][3] += r.y;
-                }
-              } else {
-                const float v = blk[(t0 / j) * sw];
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk)
-#pragma unroll
-                  for (int e = 0; e < 4; ++e) acc[kk][e] += v;
-              }
-            } else {
-              PlaneWindow<j> win;
-              win.load(stage, p, f0, t0, F);
-              float c0[4], c1[4];
-#pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                c0[e] = e < win.estar ? win.v00 : win.v01;
-                c1[e] = e < win.estar ? win.v10 : win.v11;
-              }
+          for (int e = 0; e < 4; ++e)
+            if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
+      }
+      bool flag = max16(acc) >= p.trig[0];
+      hs_sfor<MAXP - 1>([&](auto JJ) {
+        constexpr int j = decltype(JJ)::value + 2;
+        if (j <= P) {
+          const int a0 = (f0 / j) & ~3;
+          const int bw = p.bw[j], bh = p.bh[j];
+          const float *box = stage + p.soff[j];
+          const int rstep = sgn * bw;  // smem distance of staged rows r and r + 1
+          if constexpr (j == 2 || j == 4 || j == 8) {
+            const float *blk = box + (F / j - a0) + srow(t0 / j, bh, sgn) * bw;
+            if constexpr (j == 2) {
+              const float2 r0 = *reinterpret_cast<const float2 *>(blk);
+              const float2 r1 = *reinterpret_cast<const float2 *>(blk + rstep);
 #pragma unroll
               for (int kk = 0; kk < 4; ++kk) {
-                if (kk < win.kstar) {  // warp-uniform
+                const float2 r = kk < 2 ? r0 : r1;
+                acc[kk][0] += r.x; acc[kk][1] += r.x; acc[kk][2] += r.y; acc[kk][3] += r.y;
+              }
+            } else {
+              const float v = *blk;
 #pragma unroll
-                  for (int e = 0; e < 4; ++e) acc[kk][e] += c0[e];
-                } else {
+              for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-                  for (int e = 0; e < 4; ++e) acc[kk][e] += c1[e];
-                }
+                for (int e = 0; e < 4; ++e) acc[kk][e] += v;
+            }
+          } else {
+            const int rb = t0 / j;
+            const int kstar = j - (t0 - rb * j);  // first k with trunc((t0+k)/j) = rb + 1
+            const int bb = F / j;
+            const int estar = j - (F - bb * j);   // first e with (F+e)/j = bb + 1
+            const float *r0 = box + (bb - a0) + srow(rb, bh, sgn) * bw;
+            const float v00 = r0[0], v01 = r0[1], v10 = r0[rstep], v11 = r0[rstep + 1];
+            float c0[4], c1[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              c0[e] = e < estar ? v00 : v01;
+              c1[e] = e < estar ? v10 : v11;
+            }
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              if (kk < kstar) {  // warp-uniform
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[kk][e] += c0[e];
+              } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[kk][e] += c1[e];
               }
             }
-            flag |= max16(acc) >= p.trig[j - 1];
           }
-        });
-        if (flag) flags |= 1u << i;
-      }
+          flag |= max16(acc) >= p.trig[j - 1];
+        }
+      });
 
-      // ---- slow path (rare): re-walk the flagged sub-blocks of the warp
-#pragma unroll 1
-      for (int i = 0; i < 2; ++i) {
-        const bool fl = (flags >> i) & 1u;
-        if (!__any_sync(0xffffffffu, fl)) continue;
-        const int Fl = 128 * i + 4 * lane;
-        const int F = f0 + Fl;
+      // ---- slow path (rare): re-walk the cells of a warp with a flagged lane
+      if (__any_sync(0xffffffffu, flag)) {
 #pragma unroll 1
         for (int c = 0; c < 16; ++c) {
           const int kk = c >> 2, e = c & 3;
           const int t = t0 + kk;
           const int f = F + e;
-          const bool active = fl && t <= H && t >= item.tlo && f < p.n_bins;
-          const int row = H + item.sgn * t;
-          float a = active ? rows1[t * kHsBins + Fl + e] : 0.f;
+          const bool active = flag && t <= H && t >= item.tlo && f < p.n_bins;
+          const int row = H + sgn * t;
+          float a = active ? stage[p.soff[1] + srow(t, kRows1, sgn) * kHsBins + 4 * lane + e] : 0.f;
           hs_sfor<MAXP>([&](auto JJ) {
             constexpr int j = decltype(JJ)::value + 1;
             if (j <= P) {
               if constexpr (j > 1) {
                 const int a0 = (f0 / j) & ~3;
-                if (active) a += stage[p.soff[j] + (t / j) * p.sw[j] + f / j - a0];
+                if (active) a += stage[p.soff[j] + srow(t / j, p.bh[j], sgn) * p.bw[j] + f / j - a0];
               }
               const bool hit = active && a > p.hi[j - 1];
               const bool near = active && !hit && a >= p.lo[j - 1];
@@ -389,9 +376,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(HsumParams p) {
           });
         }
       }
-      // release the buffer to the producer
+      // release the stage to the producer
       __syncwarp();
-      if (lane == 0) mbar_arrive(empty + b);
+      if (lane == 0) mbar_arrive(empty + st);
     }
     warp_flush(eb, warp, wcount, p);
   }
@@ -628,18 +615,18 @@ __global__ void __launch_bounds__(1024) select_finalize_kernel(SelectParams p) {
 }
 
 // ----------------------------------------------------------------- launchers
-static int hs_warps(const HsumParams &p) { return (p.half + 1 + 3) / 4; }
+int hsum_warps(int half) { return (half + 1 + 3) / 4 <= 11 ? 11 : 16; }
+static int hsum_stages(int half) { return hsum_warps(half) == 11 ? 4 : 3; }
 
 int hsum_smem_bytes(const HsumParams &p) {
-  const int nw = hs_warps(p) <= 11 ? 11 : 16;
-  const int buf_floats = 4 * nw * kHsBins + ((p.smem_floats + 3) & ~3);
-  return 16 * 4 + 2 * buf_floats * 4 + (int)sizeof(EmitBuf);
+  return 1024 + hsum_stages(p.half) * p.stage_floats * 4 + (int)sizeof(EmitBuf);
 }
 
-template <int MAXP, int NW>
-static cudaError_t launch_hsum_t(const HsumParams &p, cudaStream_t s) {
+template <int MAXP, int NW, int STAGES>
+static cudaError_t launch_hsum_t(const HsumParams &p, const HsumMaps &m, cudaStream_t s) {
   const int smem = hsum_smem_bytes(p);
-  cudaError_t e = cudaFuncSetAttribute(hsum_kernel<MAXP, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e =
+      cudaFuncSetAttribute(hsum_kernel<MAXP, NW, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   static int n_sm = 0;
   if (!n_sm) {
@@ -648,19 +635,17 @@ static cudaError_t launch_hsum_t(const HsumParams &p, cudaStream_t s) {
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
     if (n_sm <= 0) n_sm = 1;
   }
-  const int nb = (p.n_bins + kHsBins - 1) / kHsBins;
-  const int items = nb * 2;
-  hsum_kernel<MAXP, NW><<<items < n_sm ? items : n_sm, 32 * (NW + 1), smem, s>>>(p);
+  const int items = (p.n_bins + kHsBins - 1) / kHsBins * 2;
+  hsum_kernel<MAXP, NW, STAGES><<<items < n_sm ? items : n_sm, 32 * (NW + 1), smem, s>>>(p, m);
   return cudaGetLastError();
 }
 
-cudaError_t launch_hsum(const HsumParams &p, cudaStream_t s) {
-  // warps own 4 templates each: 11 warps cover up to 87 templates, 16 up to 127
-  if (hs_warps(p) <= 11) {
-    if (p.n_planes <= 8) return launch_hsum_t<8, 11>(p, s);
-    return launch_hsum_t<16, 11>(p, s);
+cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s) {
+  if (hsum_warps(p.half) == 11) {
+    if (p.n_planes <= 8) return launch_hsum_t<8, 11, 4>(p, m, s);
+    return launch_hsum_t<16, 11, 4>(p, m, s);
   }
-  return launch_hsum_t<16, 16>(p, s);
+  return launch_hsum_t<16, 16, 3>(p, m, s);
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
