@@ -320,6 +320,7 @@ def run_ours(args):
         "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
         "stage_ms": stage_ms, "candidates": int(n_cand), "candidates_dropped": int(dropped),
         "recheck_cells": counters["recheck"], "device_status": counters["status"],
+        "selected_per_plane": counters["selected"],
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": alg[dom], "traffic": traffic},

@@ -86,7 +86,7 @@ SIGNATURES = {
     "fdas_enqueue_search_device": (_INT, [_P, _P, _P, _INT, _INT]),
     "fdas_synchronize": (_INT, [_P, _INT]),
     "fdas_get_stream": (_P, [_P, _INT]),
-    "fdas_get_counters": (_INT, [_P, _INT, _P]),
+    "fdas_get_counters": (_INT, [_P, _INT, _P, _U32]),
     "fdas_version": (ctypes.c_char_p, []),
 }
 

@@ -902,15 +902,15 @@ fdas_status fdas_get_stage_times(fdas_handle *h, fdas_buffer_set ab, float *ms6)
   return FDAS_OK;
 }
 
-fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out19) {
+fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out, uint32_t n) {
   CHECK_HANDLE(h);
   CHECK_SET(h, ab);
-  if (!out19) return fail(h, FDAS_ERR_INVALID_ARG, "out is NULL");
+  if (!out && n) return fail(h, FDAS_ERR_INVALID_ARG, "out is NULL");
   CK(h, cudaSetDevice(h->cfg.device));
   CK(h, cudaStreamSynchronize(h->set[ab].stream));
   unsigned ctrl[kCtrlWords];
   CK(h, cudaMemcpy(ctrl, h->set[ab].d_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
-  for (int i = 0; i < 3 + kMaxPlanes; ++i) out19[i] = ctrl[i];
+  for (uint32_t i = 0; i < n && i < (uint32_t)kCtrlSelLo; ++i) out[i] = ctrl[i];
   return FDAS_OK;
 }
 

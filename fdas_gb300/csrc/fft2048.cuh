@@ -326,3 +326,130 @@ __device__ __forceinline__ void fft2048_core(float2 *v, const TwiddleBases &tb, 
 }
 
 }  // namespace fdas
+
+namespace fdas {
+
+// ---------------------------------------------------------------------------
+// Two-warp inverse transform: 64 threads x 32 complex values (half the
+// registers of the one-warp form, so twice the warps per SM).
+//
+//   thread p = 32 h + l (h: warp of the pair, l: lane), input Y[64 a + p]:
+//   pass 1   Z_p[m] = DFT32_a( Y[64 a + p] ),            m in [0,32)
+//   twiddle  V_p[m] = Z_p[m] w^(m p)
+//   exchange (shared memory, across the two warps): thread (h, l) takes
+//            m = 16 h + (l & 15), g = l >> 4 and the 32 values
+//            V_{p1 + 8 p2}[m], p1 = 4 g + q (q < 4), p2 < 8
+//   pass 2a  U_{p1}[d1] = DFT8_p2(V_{p1 + 8 p2}[m]) e^(2 pi i d1 p1 / 64)
+//   exchange (register shuffle with lane l ^ 16): each thread keeps four d1
+//            values for all eight p1
+//   pass 2c  y[m + 32 d1 + 256 d2] = DFT8_p1( U_{p1}[d1] )
+//
+// Lanes with g = 1 modulate their pass-2a inputs by (-1)^p2, which moves
+// their own d1 half (4..7) into register slots 0..3, so the shuffle pattern is
+// the same for all lanes; they then feed their p1 halves to the last DFT8 in
+// swapped order, which multiplies the outputs by (-1)^d2 -- harmless, since
+// only |y|^2 is used.  The result is therefore given as |y|^2 only.
+constexpr int kEx2Pitch = 33;                 // complex values per row of the pair buffer
+constexpr int kEx2Floats = 64 * kEx2Pitch * 2;  // floats per warp pair (>= 2048 complex)
+
+struct Twiddle2 {
+  float2 lo[4];  // w^(p k1), k1 < 4
+  float2 hi[8];  // w^(4 p k2), k2 < 8
+};
+
+__device__ __forceinline__ Twiddle2 load_twiddle2(const float2 *__restrict__ table, int p) {
+  Twiddle2 t;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) t.lo[k] = __ldg(table + ((k * p) & 2047));
+#pragma unroll
+  for (int k = 0; k < 8; ++k) t.hi[k] = __ldg(table + ((4 * k * p) & 2047));
+  return t;
+}
+
+// Pass 1 + twiddle + write to the pair buffer.  v[a] holds Y[64 a + p] on entry.
+__device__ __forceinline__ void ifft2_pass1(float2 *v, const Twiddle2 &tw, float2 *buf, int p) {
+  dft32<+1, 0>(v);
+  // V_p[m] = Z_p[m] w^(m p), m = k1 + 4 k2 sits in v[8 k1 + k2]
+  sfor<4>([&](auto K1) {
+    constexpr int k1 = decltype(K1)::value;
+    sfor<8>([&](auto K2) {
+      constexpr int k2 = decltype(K2)::value;
+      constexpr int idx = 8 * k1 + k2;
+      if constexpr (k1 == 0 && k2 == 0) {
+      } else if constexpr (k1 == 0) {
+        v[idx] = cmul(v[idx], tw.hi[k2]);
+      } else if constexpr (k2 == 0) {
+        v[idx] = cmul(v[idx], tw.lo[k1]);
+      } else {
+        v[idx] = cmul(v[idx], cmul(tw.lo[k1], tw.hi[k2]));
+      }
+    });
+  });
+  float2 *row = buf + kEx2Pitch * p;
+  sfor<32>([&](auto M) {
+    constexpr int m = decltype(M)::value;
+    row[m] = v[pos32(m)];
+  });
+}
+
+// Passes 2a / 2c after the pair buffer has been written by both warps.  On
+// exit pw[8 r + d2] holds |y[m + 32 (4 g + r) + 256 d2]|^2, m = 16 h + (l & 15).
+template <typename Hook>
+__device__ __forceinline__ void ifft2_pass2(const float2 *buf, int h, int lane, float *pw, Hook after_read) {
+  const int m = 16 * h + (lane & 15);
+  const int g = lane >> 4;
+  float2 u[32];  // u[8 q + p2]
+  sfor<4>([&](auto Q) {
+    constexpr int q = decltype(Q)::value;
+    sfor<8>([&](auto P2) {
+      constexpr int p2 = decltype(P2)::value;
+      u[8 * q + p2] = buf[kEx2Pitch * (4 * g + q + 8 * p2) + m];
+    });
+  });
+  after_read();
+  // lanes of group 1: (-1)^p2 modulation moves d1 = 4..7 to slots 0..3
+  const float sg = g ? -1.f : 1.f;
+  sfor<4>([&](auto Q) {
+    constexpr int q = decltype(Q)::value;
+    sfor<4>([&](auto P2) {
+      constexpr int p2 = 2 * decltype(P2)::value + 1;
+      u[8 * q + p2] = make_float2(sg * u[8 * q + p2].x, sg * u[8 * q + p2].y);
+    });
+    dft8<+1, 8 * q, 1>(u);
+    // twiddle e^(2 pi i d1 p1 / 64); constants differ per lane group
+    sfor<8>([&](auto D) {
+      constexpr int d = decltype(D)::value;
+      constexpr float c0r = kCos<64, ((d & 7) * q)>, c0i = kSin<64, ((d & 7) * q)>;
+      constexpr float c1r = kCos<64, (((d + 4) & 7) * (4 + q))>, c1i = kSin<64, (((d + 4) & 7) * (4 + q))>;
+      const float2 c = make_float2(g ? c1r : c0r, g ? c1i : c0i);
+      u[8 * q + d] = cmul(u[8 * q + d], c);
+    });
+  });
+  // exchange with lane ^ 16: send slots 4..7, receive the partner's, in place
+  sfor<4>([&](auto Q) {
+    constexpr int q = decltype(Q)::value;
+    sfor<4>([&](auto R) {
+      constexpr int r = decltype(R)::value;
+      float2 &x = u[8 * q + 4 + r];
+      x.x = __shfl_xor_sync(0xffffffffu, x.x, 16);
+      x.y = __shfl_xor_sync(0xffffffffu, x.y, 16);
+    });
+  });
+  // pass 2c: for each own d1 slot r, DFT8 over p1 = (own q = 0..3, partner q = 0..3)
+  sfor<4>([&](auto R) {
+    constexpr int r = decltype(R)::value;
+    float2 x[8];
+    sfor<4>([&](auto Q) {
+      constexpr int q = decltype(Q)::value;
+      x[q] = u[8 * q + r];
+      x[4 + q] = u[8 * q + 4 + r];
+    });
+    dft8<+1, 0, 1>(x);
+    sfor<8>([&](auto D2) {
+      constexpr int d2 = decltype(D2)::value;
+      pw[8 * r + d2] = fmaf(x[d2].x, x[d2].x, x[d2].y * x[d2].y);
+    });
+  });
+}
+
+}  // namespace fdas

@@ -1,5 +1,8 @@
 // (a) overlap-save tiling + forward FFT, (c) fused template multiply,
 // inverse FFT, power and overlap discard, and the FP64 template precompute.
+#include <cstdlib>
+#include <cstring>
+
 #include "fft2048.cuh"
 #include "kernels.cuh"
 
@@ -149,6 +152,98 @@ __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Two-warp variant: one warp pair per (tile, template) item, 32 values per
+// thread (<= 128 registers, two CTAs of 4 pairs per SM).  The pair buffer
+// (16.9 KB) holds the TMA-prefetched template spectrum of the item, then the
+// pass-1 exchange; the next item's template is prefetched into it as soon as
+// both warps have read the exchange back.
+constexpr int kPairsPerCta = 4;
+
+__device__ __forceinline__ void pair_sync(int pair) {
+  asm volatile("bar.sync %0, %1;" ::"r"(pair + 1), "r"(64) : "memory");
+}
+// barrier over the pair that also ANDs a predicate across its 64 threads
+__device__ __forceinline__ bool pair_and(int pair, bool v) {
+  unsigned r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, %2, %3, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((unsigned)v), "r"(pair + 1), "r"(64)
+      : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
+  extern __shared__ float4 smem_f4[];
+  __shared__ uint64_t bars[kPairsPerCta];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pair = warp >> 1, h = warp & 1;
+  const int tp = 32 * h + lane;  // thread of the pair
+  float *buf_f = reinterpret_cast<float *>(smem_f4) + pair * kEx2Floats;
+  float2 *buf = reinterpret_cast<float2 *>(buf_f);
+  uint64_t *bar = &bars[pair];
+  const int n_items = p.n_tiles * p.n_rows;
+  const int stride = gridDim.x * kPairsPerCta;
+  int item = blockIdx.x * kPairsPerCta + pair;
+  if (tp == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  pair_sync(pair);
+  const Twiddle2 tw = load_twiddle2(p.twiddle, tp);
+  if (item < n_items && tp == 0)
+    prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + item % p.n_rows) * kTile, bar);
+  uint32_t parity = 0;
+  const int m = 16 * h + (lane & 15);
+  const int g = lane >> 4;
+  for (; item < n_items; item += stride) {
+    const int tile = item / p.n_rows;
+    const int row = p.row_begin + (item - tile * p.n_rows);
+    const float2 *s = p.tiles + (long long)tile * kTile + tp;
+    float2 v[32];
+    sfor<32>([&](auto A) {
+      constexpr int a = decltype(A)::value;
+      v[a] = __ldg(s + 64 * a);
+    });
+    // the decision to go on is made uniform over the pair
+    if (!pair_and(pair, mbar_wait(bar, parity, p.timeout_ns))) {
+      if (tp == 0) atomicOr(p.status, kStatusFtcTimeout);
+      mbar_wait(bar, parity, p.timeout_ns);  // bounded: let the copy land before exiting
+      return;
+    }
+    parity ^= 1u;
+    sfor<32>([&](auto A) {
+      constexpr int a = decltype(A)::value;
+      v[a] = cmul(v[a], buf[64 * a + tp]);
+    });
+    pair_sync(pair);  // template read by both warps: the buffer takes the exchange
+    ifft2_pass1(v, tw, buf, tp);
+    pair_sync(pair);  // exchange written
+    const int next = item + stride;
+    float pw[32];
+    ifft2_pass2(buf, h, lane, pw, [&]() {
+      pair_sync(pair);  // exchange read by both warps: prefetch the next template
+      if (next < n_items && tp == 0)
+        prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
+    });
+    float *out = p.fop + (long long)row * p.fop_stride;
+    const long long base = (long long)tile * p.payload - p.overlap;
+    sfor<4>([&](auto R) {
+      constexpr int r = decltype(R)::value;
+      sfor<8>([&](auto D2) {
+        constexpr int d2 = decltype(D2)::value;
+        const int n = m + 32 * (4 * g + r) + 256 * d2;
+        const long long b = base + n;
+        if (n >= p.overlap && b < p.n_bins) out[b] = pw[8 * r + d2];
+      });
+    });
+  }
+}
+
 // FP64 DFT of the time-domain taps -> float spectra scaled by 2^-11.
 __global__ void spectra_kernel(SpectraParams p) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -200,14 +295,18 @@ cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
-  static bool attr = false;
-  const int smem = ex_smem_bytes();
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(ftc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
+// FFT variant of the FT convolution: the two-warp form (default) or the
+// one-warp form; FDAS_FTC_VARIANT=1warp selects the latter.
+static int ftc_variant() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("FDAS_FTC_VARIANT");
+    v = (e && strcmp(e, "1warp") == 0) ? 1 : 2;
   }
+  return v;
+}
+
+cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
   if (p.n_rows <= 0 || p.n_tiles <= 0) return cudaSuccess;
   static int n_sm = 0;
   if (!n_sm) {
@@ -217,8 +316,19 @@ cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
     if (n_sm <= 0) n_sm = 1;
   }
   const long long items = (long long)p.n_tiles * p.n_rows;
-  const long long ctas = (items + kWarpsPerCta - 1) / kWarpsPerCta;
-  ftc_kernel<<<(int)(ctas < n_sm ? ctas : n_sm), 256, smem, s>>>(p);
+  if (ftc_variant() == 1) {
+    const int smem = ex_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(ftc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const long long ctas = (items + kWarpsPerCta - 1) / kWarpsPerCta;
+    ftc_kernel<<<(int)(ctas < n_sm ? ctas : n_sm), 256, smem, s>>>(p);
+  } else {
+    const int smem = kPairsPerCta * kEx2Floats * (int)sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(ftc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const long long ctas = (items + kPairsPerCta - 1) / kPairsPerCta;
+    ftc2_kernel<<<(int)(ctas < 2 * n_sm ? ctas : 2 * n_sm), 256, smem, s>>>(p);
+  }
   return cudaGetLastError();
 }
 

@@ -207,6 +207,26 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
 // boxes hold FOP rows in ascending order, i.e. reversed for the negative half
 __device__ __forceinline__ int srow(int r, int bh, int sgn) { return sgn > 0 ? r : bh - 1 - r; }
 
+// Emission of plane j (0-based `plane`) straight from the accumulators: called
+// by the whole warp when some lane's tile reached the lower edge of the band.
+__device__ __forceinline__ void emit_plane(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
+                                           const float (&acc)[4][4], int plane, int H, int sgn, int t0, int F) {
+  const float hi = p.hi[plane], lo = p.lo[plane];
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float a = acc[kk][e];  // -inf for masked cells
+      const bool hit = a > hi;
+      const bool near = !hit && a >= lo;
+      const unsigned hm = __ballot_sync(0xffffffffu, hit);
+      if (hm) warp_emit(eb, warp, wcount, p, hm, plane, H + sgn * (t0 + kk), F + e, a);
+      const unsigned nm = __ballot_sync(0xffffffffu, near);
+      if (nm) warp_recheck(p, nm, plane, H + sgn * (t0 + kk), F + e);
+    }
+  }
+}
+
 template <int MAXP, int NW, int kHsStages>
 __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_constant__ HsumParams p,
                                                                  const __grid_constant__ HsumMaps m) {
@@ -296,7 +316,8 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_con
           for (int e = 0; e < 4; ++e)
             if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
       }
-      bool flag = max16(acc) >= p.trig[0];
+      if (__any_sync(0xffffffffu, max16(acc) >= p.trig[0]))
+        emit_plane(eb, warp, wcount, p, acc, 0, H, sgn, t0, F);
       hs_sfor<MAXP - 1>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value + 2;
         if (j <= P) {
@@ -345,37 +366,12 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_con
               }
             }
           }
-          flag |= max16(acc) >= p.trig[j - 1];
+          // rare: some lane of the warp reached the band of plane j
+          if (__any_sync(0xffffffffu, max16(acc) >= p.trig[j - 1]))
+            emit_plane(eb, warp, wcount, p, acc, j - 1, H, sgn, t0, F);
         }
       });
 
-      // ---- slow path (rare): re-walk the cells of a warp with a flagged lane
-      if (__any_sync(0xffffffffu, flag)) {
-#pragma unroll 1
-        for (int c = 0; c < 16; ++c) {
-          const int kk = c >> 2, e = c & 3;
-          const int t = t0 + kk;
-          const int f = F + e;
-          const bool active = flag && t <= H && t >= item.tlo && f < p.n_bins;
-          const int row = H + sgn * t;
-          float a = active ? stage[p.soff[1] + srow(t, kRows1, sgn) * kHsBins + 4 * lane + e] : 0.f;
-          hs_sfor<MAXP>([&](auto JJ) {
-            constexpr int j = decltype(JJ)::value + 1;
-            if (j <= P) {
-              if constexpr (j > 1) {
-                const int a0 = (f0 / j) & ~3;
-                if (active) a += stage[p.soff[j] + srow(t / j, p.bh[j], sgn) * p.bw[j] + f / j - a0];
-              }
-              const bool hit = active && a > p.hi[j - 1];
-              const bool near = active && !hit && a >= p.lo[j - 1];
-              const unsigned hm = __ballot_sync(0xffffffffu, hit);
-              if (hm) warp_emit(eb, warp, wcount, p, hm, j - 1, row, f, a);
-              const unsigned nm = __ballot_sync(0xffffffffu, near);
-              if (nm) warp_recheck(p, nm, j - 1, row, f);
-            }
-          });
-        }
-      }
       // release the stage to the producer
       __syncwarp();
       if (lane == 0) mbar_arrive(empty + st);
@@ -388,25 +384,26 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_con
   if (threadIdx.x < P && eb.pc[threadIdx.x]) atomicAdd(p.cand_count + threadIdx.x, eb.pc[threadIdx.x]);
 }
 
-// One warp per recheck entry: HP_j of the cell in FP64 from the spectrum and
-// the FP64 taps, FOP(r, g) = |sum_q X[g - q] h_r[q]|^2 (ft_conv.py:201-205).
-__global__ void __launch_bounds__(256) recheck_kernel(RecheckParams p) {
-  const int lane = threadIdx.x & 31;
+// FP64 recheck: a CTA per entry (grid-stride), warp j computes the FP64 FOP
+// cell FOP(trunc(t/(j+1)), bin/(j+1)) = |sum_q X[g - q] h_r[q]|^2
+// (ft_conv.py:201-205) with its lanes over the taps; warp 0 then sums the
+// planes in order j = 1..k (hsum.py:95-120) and compares with the threshold.
+__global__ void __launch_bounds__(512) recheck_kernel(RecheckParams p) {
+  __shared__ double cell[kMaxPlanes];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
   const unsigned n = min(*p.rc_count, (unsigned)p.rc_cap);
-  const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (unsigned e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < n; e += nwarps) {
+  for (unsigned e = blockIdx.x; e < n; e += gridDim.x) {
     const uint4 ent = p.rc_list[e];
     const int plane = (int)ent.x, row = (int)ent.y, bin = (int)ent.z;
     const int t = row - p.half;
-    double hp = 0.0;
-    for (int j = 1; j <= plane + 1; ++j) {
+    for (int j = warp + 1; j <= plane + 1; j += nwarps) {
       const int tj = (t >= 0) ? t / j : -((-t) / j);
       const int r = p.half + tj;
       const int g = bin / j;
-      const int len = p.tap_len[r];
+      const int qn = min(p.tap_len[r], g + 1);
       const double2 *h = p.taps + (long long)r * p.tap_pitch;
       double re = 0.0, im = 0.0;
-      const int qn = min(len, g + 1);
 #pragma unroll 4
       for (int q = lane; q < qn; q += 32) {
         const float2 x = p.input[g - q];
@@ -419,13 +416,19 @@ __global__ void __launch_bounds__(256) recheck_kernel(RecheckParams p) {
         re += __shfl_xor_sync(0xffffffffu, re, o);
         im += __shfl_xor_sync(0xffffffffu, im, o);
       }
-      hp += re * re + im * im;
+      if (lane == 0) cell[j - 1] = re * re + im * im;
     }
-    if (lane == 0 && hp > p.thr[plane]) {
-      atomicAdd(p.cand_count + plane, 1u);
-      global_append(p.cand_key, p.cand_pwr, p.cand_total, p.cand_cap, p.status, cand_key(plane, row, bin),
-                    (float)hp);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double hp = 0.0;
+      for (int j = 0; j <= plane; ++j) hp += cell[j];
+      if (hp > p.thr[plane]) {
+        atomicAdd(p.cand_count + plane, 1u);
+        global_append(p.cand_key, p.cand_pwr, p.cand_total, p.cand_cap, p.status, cand_key(plane, row, bin),
+                      (float)hp);
+      }
     }
+    __syncthreads();
   }
 }
 
@@ -649,7 +652,7 @@ cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s) 
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
-  recheck_kernel<<<2 * 152, 256, 0, s>>>(p);
+  recheck_kernel<<<2 * 152, 32 * 8, 0, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -229,12 +229,12 @@ class FDAS:
     def counters(self, ab):
         """Device counters of the last harmonic summing: dict with status,
         recheck (cells sent to the FP64 recheck), records and per-plane hits."""
-        out = np.zeros(19, dtype=np.uint32)
-        if not self._check(self._lib.fdas_get_counters(self._h, int(ab), _ptr(out)), "get_counters"):
+        out = np.zeros(35, dtype=np.uint32)
+        if not self._check(self._lib.fdas_get_counters(self._h, int(ab), _ptr(out), out.size), "get_counters"):
             return None
         n = self.config.n_planes
         return {"status": int(out[0]), "recheck": int(out[1]), "records": int(out[2]),
-                "per_plane": [int(x) for x in out[3:3 + n]]}
+                "per_plane": [int(x) for x in out[3:3 + n]], "selected": [int(x) for x in out[19:19 + n]]}
 
     def stage_times(self, ab):
         ms = np.zeros(6, dtype=np.float32)

@@ -231,11 +231,12 @@ fdas_status fdas_synchronize(fdas_handle *h, fdas_buffer_set ab);
 /* The CUDA stream (cudaStream_t) of buffer set `ab`. */
 void *fdas_get_stream(fdas_handle *h, fdas_buffer_set ab);
 
-/* Device counters of the last harmonic summing on `ab` (blocking):
+/* Device counters of the last search on `ab` (blocking), up to `n` words:
  * [0] status bits (1 staging timeout, 2 recheck list full, 4 candidate list
- * full, 8 selection buffer full), [1] cells sent to the FP64 recheck,
- * [2] candidate records appended, [3 + p] hits of plane p (p < 16). */
-fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out19);
+ * full, 8 selection buffer full, 16 FT-convolution timeout), [1] cells sent
+ * to the FP64 recheck, [2] candidate records appended, [3 + p] hits of plane
+ * p, [19 + p] records gathered for plane p's fixed-size list (p < 16). */
+fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out, uint32_t n);
 
 /* Library version string. */
 const char *fdas_version(void);
