@@ -33,7 +33,8 @@ constexpr int kCtrlCount = 3;                       // + plane: hits per plane
 constexpr int kCtrlSelCount = kCtrlCount + kMaxPlanes;
 constexpr int kCtrlSelLo = kCtrlSelCount + kMaxPlanes;
 constexpr int kCtrlItems = kCtrlSelLo + kMaxPlanes;  // harmonic-summing work counter
-constexpr int kCtrlWords = kCtrlItems + 1;
+constexpr int kCtrlBound = kCtrlItems + 1;           // + plane: boundary records of the selection
+constexpr int kCtrlWords = kCtrlBound + kMaxPlanes;
 constexpr uint32_t kDefaultCapacity = 1u << 22;     // candidate records per buffer set
 constexpr uint32_t kMaxCapacity = 1u << 27;
 constexpr int kRecheckCap = 65536;
@@ -54,6 +55,7 @@ struct BufferSet {
   unsigned *h_ctrl = nullptr;  // pinned mirror of d_ctrl
   uint4 *d_rc = nullptr;
   unsigned *d_hist = nullptr;
+  unsigned *d_ticket = nullptr;
   unsigned long long *d_sel_key = nullptr;
   float *d_sel_pwr = nullptr;
   uint32_t *d_cloc = nullptr;
@@ -311,8 +313,6 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
       p.trig[j] = t;
     }
   }
-  int off = 0;
-  unsigned bytes = 0;
   hsum_geometry(h, p);
   p.item_counter = S.d_ctrl + kCtrlItems;
   p.cand_key = S.d_key;
@@ -359,10 +359,12 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   f.n_planes = P;
   f.per_plane = h->per_plane;
   f.hist = S.d_hist;
-  f.sel_lo = S.d_ctrl + kCtrlSelLo;
+  f.ticket = S.d_ticket;
+  f.sel_bucket = reinterpret_cast<int *>(S.d_ctrl + kCtrlSelLo);
+  f.sure_count = S.d_ctrl + kCtrlSelCount;
+  f.bound_count = S.d_ctrl + kCtrlBound;
   f.sel_key = S.d_sel_key;
   f.sel_pwr = S.d_sel_pwr;
-  f.sel_count = S.d_ctrl + kCtrlSelCount;
   f.compat_loc = S.d_cloc;
   f.compat_pwr = S.d_cpwr;
   f.invalid_location = (uint32_t)((h->H + 1 + h->H) & 0x7f) << 22;  // encode(1, H+1, 0), gen_info.h:69
@@ -423,6 +425,7 @@ void free_set(BufferSet &S) {
   cudaFree(S.d_ctrl);
   cudaFree(S.d_rc);
   cudaFree(S.d_hist);
+  cudaFree(S.d_ticket);
   cudaFree(S.d_sel_key);
   cudaFree(S.d_sel_pwr);
   cudaFree(S.d_cloc);
@@ -479,7 +482,8 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
   uint32_t cap = cfg.candidate_capacity ? cfg.candidate_capacity : kDefaultCapacity;
   if (cap > kMaxCapacity) return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidate_capacity must be <= 2^27");
   uint32_t pc = cfg.candidates_per_plane_compat ? cfg.candidates_per_plane_compat : 512u;
-  if (pc > (uint32_t)kSortCap) return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidates_per_plane_compat must be <= 8192");
+  if (pc > (uint32_t)kMaxCompat)
+    return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidates_per_plane_compat must be <= 2048");
 
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -555,8 +559,9 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
         {(void **)&S.d_ctrl, sizeof(unsigned) * kCtrlWords},
         {(void **)&S.d_rc, sizeof(uint4) * kRecheckCap},
         {(void **)&S.d_hist, sizeof(unsigned) * (size_t)h->P * kSelBuckets},
-        {(void **)&S.d_sel_key, sizeof(unsigned long long) * (size_t)h->P * kSortCap},
-        {(void **)&S.d_sel_pwr, sizeof(float) * (size_t)h->P * kSortCap},
+        {(void **)&S.d_ticket, sizeof(unsigned)},
+        {(void **)&S.d_sel_key, sizeof(unsigned long long) * (size_t)h->P * 2 * kSortCap},
+        {(void **)&S.d_sel_pwr, sizeof(float) * (size_t)h->P * 2 * kSortCap},
         {(void **)&S.d_cloc, sizeof(uint32_t) * (size_t)h->P * h->per_plane},
         {(void **)&S.d_cpwr, sizeof(float) * (size_t)h->P * h->per_plane},
     };
@@ -570,6 +575,7 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
     }
     if ((e = cudaMemset(S.d_fop, 0, sizeof(float) * fop_floats)) != cudaSuccess ||
         (e = cudaMemset(S.d_hist, 0, sizeof(unsigned) * (size_t)h->P * kSelBuckets)) != cudaSuccess ||
+        (e = cudaMemset(S.d_ticket, 0, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMemset(S.d_ctrl, 0, sizeof(unsigned) * kCtrlWords)) != cudaSuccess ||
         (e = cudaHostAlloc((void **)&S.h_ctrl, sizeof(unsigned) * kCtrlWords, cudaHostAllocDefault)) !=
             cudaSuccess ||

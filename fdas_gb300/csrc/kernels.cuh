@@ -10,9 +10,10 @@ namespace fdas {
 constexpr int kTile = 2048;          // FFT / tile size (gen_info.h:33, 42)
 constexpr int kMaxPlanes = 16;       // harmonic planes supported by the kernels
 constexpr int kHsBins = 128;         // bins per harmonic-summing work item
-constexpr int kSortCap = 8192;       // records one CTA sorts in shared memory
+constexpr int kSortCap = 8192;       // boundary records one CTA ranks in shared memory
+constexpr int kMaxCompat = 2048;     // entries per plane of the fixed-size list
 constexpr int kEmitBuf = 1024;       // candidate records staged per harmonic-summing CTA
-constexpr int kSelBuckets = 65536;   // power buckets of the top-K selection (top 16 key bits)
+constexpr int kSelBuckets = 2048;    // power buckets of the top-K selection (float bits 30..20)
 
 // device status bits (per buffer set)
 constexpr int kStatusHsumTimeout = 1;
@@ -122,11 +123,13 @@ struct SelectParams {
   int cand_cap;
   int n_planes;
   int per_plane;          // K: entries per plane in the fixed-size list
-  unsigned *hist;         // [plane][kSelBuckets]
-  unsigned *sel_lo;       // [plane] lowest power key taken
-  unsigned long long *sel_key;  // [plane][kSortCap]
-  float *sel_pwr;         // [plane][kSortCap]
-  unsigned *sel_count;    // [plane]
+  unsigned *hist;         // [plane][kSelBuckets], left zeroed after use
+  unsigned *ticket;       // last-block detection of the histogram kernel
+  int *sel_bucket;        // [plane] boundary bucket (-1: take every hit)
+  unsigned *sure_count;   // [plane] records above the boundary bucket
+  unsigned *bound_count;  // [plane] records in the boundary bucket
+  unsigned long long *sel_key;  // [plane][2][kSortCap]: sure list, boundary list
+  float *sel_pwr;
   uint32_t *compat_loc;   // [plane][per_plane]
   float *compat_pwr;
   uint32_t invalid_location;

@@ -209,8 +209,10 @@ __device__ __forceinline__ int srow(int r, int bh, int sgn) { return sgn > 0 ? r
 
 // Emission of plane j (0-based `plane`) straight from the accumulators: called
 // by the whole warp when some lane's tile reached the lower edge of the band.
-__device__ __forceinline__ void emit_plane(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
-                                           const float (&acc)[4][4], int plane, int H, int sgn, int t0, int F) {
+// Kept out of line: it runs rarely and would otherwise be inlined once per
+// plane, which blows the instruction cache of the hot loop.
+__device__ __noinline__ void emit_plane(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
+                                        const float (&acc)[4][4], int plane, int H, int sgn, int t0, int F) {
   const float hi = p.hi[plane], lo = p.lo[plane];
 #pragma unroll
   for (int kk = 0; kk < 4; ++kk) {
@@ -255,6 +257,12 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_con
   if (warp == NW) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
+      // items are taken from the global counter in chunks of kChunk, and the
+      // next chunk is requested one chunk ahead so the atomic's latency is hidden
+      constexpr int kChunk = 4;
+      int cur = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
+      int nxt = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
+      int used = 0;
       for (int s = 0;; ++s) {
         const int st = s % kHsStages, use = s / kHsStages;
         if (use >= 1 && !mbar_wait_parity(empty + st, (use - 1) & 1, p.timeout_ns)) {
@@ -263,7 +271,12 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_con
           mbar_arrive(full + st);
           break;
         }
-        const int it = (int)atomicAdd(p.item_counter, 1u);
+        if (used == kChunk) {
+          cur = nxt;
+          used = 0;
+          if (cur < n_items) nxt = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
+        }
+        const int it = cur + used++;
         if (it >= n_items) {
           item_id[st] = -1;
           mbar_arrive(full + st);  // plain arrival: the stage carries the stop mark
@@ -435,109 +448,85 @@ __global__ void __launch_bounds__(512) recheck_kernel(RecheckParams p) {
 // ------------------------------------------- deterministic top-K per plane
 // The fixed-size list keeps, per plane, the K strongest hits (power
 // descending, location ascending on ties) in location order.  Hits are stored
-// unordered by the harmonic-summing CTAs; the selection is a radix select on
-// the power: a histogram of the top 16 bits of each plane's power keys, the
-// bucket where the count from the top reaches K, a gather of the records at or
-// above that bucket, and a one-CTA sort of the gathered records.
+// unordered by the harmonic-summing kernel.  Selection: a histogram of each
+// plane's powers over 2048 buckets (float bits 30..20, powers are >= 0) built
+// in shared memory per CTA; the last CTA finds the bucket where the count from
+// the top reaches K; the records above it ("sure") and in it ("boundary") are
+// gathered; one CTA per plane ranks the boundary records and then orders the
+// kept ones by location, both by direct rank computation.
 
-// order-preserving map of a float to an unsigned key
-__device__ __forceinline__ unsigned float_key(float f) {
-  const unsigned u = __float_as_uint(f);
-  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
+__device__ __forceinline__ int pwr_bucket(float pw) { return (int)((__float_as_uint(pw) >> 20) & 0x7ffu); }
 
-__device__ __forceinline__ unsigned stored_records(const SelectParams &p) {
-  return min(*p.cand_total, (unsigned)p.cand_cap);
-}
-
-__global__ void __launch_bounds__(256) select_hist_kernel(SelectParams p) {
-  const unsigned n = stored_records(p);
+__global__ void __launch_bounds__(1024) select_hist_kernel(SelectParams p) {
+  extern __shared__ unsigned sh_hist[];  // [n_planes][kSelBuckets]
+  __shared__ bool last;
+  const int nb = p.n_planes * kSelBuckets;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sh_hist[i] = 0u;
+  __syncthreads();
+  const unsigned n = min(*p.cand_total, (unsigned)p.cand_cap);
+  const unsigned K = (unsigned)p.per_plane;
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int plane = (int)(p.cand_key[i] >> 48);
-    if (p.cand_count[plane] > (unsigned)p.per_plane) {
-      const unsigned idx = (unsigned)plane * kSelBuckets + (float_key(p.cand_pwr[i]) >> 16);
-      // records of similar power share buckets: one atomic per distinct bucket of the warp
-      const unsigned peers = __match_any_sync(__activemask(), idx);
-      if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(p.hist + idx, (unsigned)__popc(peers));
-    }
+    if (p.cand_count[plane] > K) atomicAdd(sh_hist + plane * kSelBuckets + pwr_bucket(p.cand_pwr[i]), 1u);
   }
-}
-
-// One CTA (32 warps) per plane.  Warp w owns the 2048 buckets
-// [kSelBuckets - 2048 (w+1), kSelBuckets - 2048 w) (warp 0 the strongest);
-// all reads are coalesced.  The warp whose segment holds the K-th strongest
-// record scans it 32 buckets at a time from the top.
-__global__ void __launch_bounds__(1024) select_threshold_kernel(SelectParams p) {
-  __shared__ unsigned seg[32];
-  const int plane = blockIdx.x;
-  unsigned *h = p.hist + (size_t)plane * kSelBuckets;
-  const unsigned K = (unsigned)p.per_plane;
-  if (p.cand_count[plane] <= K) {
-    if (threadIdx.x == 0) p.sel_lo[plane] = 0u;
-    return;
-  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x)
+    if (sh_hist[i]) atomicAdd(p.hist + i, sh_hist[i]);
+  // the last CTA to finish picks the boundary bucket of every plane
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(p.ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int kSeg = kSelBuckets / 32;
-  const int top = kSelBuckets - kSeg * warp;  // exclusive
-  unsigned local = 0;
-  for (int b = top - 1 - lane; b >= top - kSeg; b -= 32) local += h[b];
+  if (warp < p.n_planes) {
+    const int plane = warp;
+    if (p.cand_count[plane] <= K) {
+      if (lane == 0) p.sel_bucket[plane] = -1;
+    } else {
+      volatile unsigned *h = p.hist + plane * kSelBuckets;
+      // strongest first: chunk c covers buckets [2048 - 32 (c+1), 2048 - 32 c)
+      unsigned above = 0;
+      int found = -1;
+      for (int c = 0; c < kSelBuckets / 32 && found < 0; ++c) {
+        const int b = kSelBuckets - 1 - 32 * c - lane;
+        unsigned v = h[b];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-  if (lane == 0) seg[warp] = local;
-  __syncthreads();
-  if (warp == 0) {
-    // inclusive scan of the segment totals, strongest first
-    unsigned v = seg[lane];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned u = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += u;
-    }
-    const unsigned before = __shfl_up_sync(0xffffffffu, v, 1);
-    seg[lane] = lane ? before : 0u;  // exclusive prefix
-    const unsigned crossing = __ballot_sync(0xffffffffu, v >= K);
-    if (lane == 0 && !crossing) p.sel_lo[plane] = 0u;  // fewer stored than K (overflow): take all
-  }
-  __syncthreads();
-  const unsigned before = seg[warp];
-  const unsigned after = (warp < 31) ? seg[warp + 1] : 0xffffffffu;
-  if (before < K && (warp == 31 || after >= K)) {
-    // this warp's segment holds the crossing
-    unsigned c = before;
-    for (int chunk = top; chunk > top - kSeg; chunk -= 32) {
-      const int b = chunk - 1 - lane;  // lane 0 = strongest of the chunk
-      unsigned v = h[b];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned u = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += u;
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned u = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += u;
+        }
+        const unsigned hit = __ballot_sync(0xffffffffu, above + v >= K);
+        if (hit) found = kSelBuckets - 1 - 32 * c - (__ffs(hit) - 1);
+        else above += __shfl_sync(0xffffffffu, v, 31);
       }
-      const unsigned hit = __ballot_sync(0xffffffffu, c + v >= K);
-      if (hit) {
-        const int l = __ffs(hit) - 1;
-        if (lane == 0) p.sel_lo[plane] = (unsigned)(chunk - 1 - l) << 16;
-        break;
-      }
-      c += __shfl_sync(0xffffffffu, v, 31);
+      if (lane == 0) p.sel_bucket[plane] = found;  // -1: fewer stored than K (overflow), take all
     }
   }
   __syncthreads();
-  // leave the histogram zeroed for the next search
-  for (int b = top - 1 - lane; b >= top - kSeg; b -= 32)
-    if (h[b]) h[b] = 0u;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) p.hist[i] = 0u;
+  if (threadIdx.x == 0) *p.ticket = 0u;
 }
 
 __global__ void __launch_bounds__(256) select_gather_kernel(SelectParams p) {
-  const unsigned n = stored_records(p);
+  const unsigned n = min(*p.cand_total, (unsigned)p.cand_cap);
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const unsigned long long key = p.cand_key[i];
     const int plane = (int)(key >> 48);
     const float pw = p.cand_pwr[i];
-    if (float_key(pw) >= p.sel_lo[plane]) {
-      const unsigned idx = atomicAdd(p.sel_count + plane, 1u);
+    const int sb = p.sel_bucket[plane];
+    const int b = pwr_bucket(pw);
+    int list = -1;
+    unsigned *cnt = nullptr;
+    if (sb < 0 || b > sb) { list = 0; cnt = p.sure_count + plane; }
+    else if (b == sb) { list = 1; cnt = p.bound_count + plane; }
+    if (list >= 0) {
+      const unsigned idx = atomicAdd(cnt, 1u);
       if (idx < (unsigned)kSortCap) {
-        p.sel_key[(size_t)plane * kSortCap + idx] = key;
-        p.sel_pwr[(size_t)plane * kSortCap + idx] = pw;
+        const size_t o = ((size_t)plane * 2 + list) * kSortCap + idx;
+        p.sel_key[o] = key;
+        p.sel_pwr[o] = pw;
       } else {
         atomicOr(p.status, kStatusSelectionOverflow);
       }
@@ -545,75 +534,62 @@ __global__ void __launch_bounds__(256) select_gather_kernel(SelectParams p) {
   }
 }
 
-struct Rec {
-  unsigned long long key;
-  float pwr;
-};
-
-__device__ __forceinline__ bool less_key(const Rec &a, const Rec &b) { return a.key < b.key; }
-// "stronger first": power descending, key ascending on ties
-__device__ __forceinline__ bool less_pwr(const Rec &a, const Rec &b) {
-  return (a.pwr > b.pwr) || (a.pwr == b.pwr && a.key < b.key);
-}
-
-template <bool BY_PWR>
-__device__ void bitonic_sort(unsigned long long *keys, float *pwrs, int m) {
-  for (int k = 2; k <= m; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        const int ixj = i ^ j;
-        if (ixj > i) {
-          Rec a{keys[i], pwrs[i]}, b{keys[ixj], pwrs[ixj]};
-          const bool up = (i & k) == 0;
-          const bool swap = up ? (BY_PWR ? less_pwr(b, a) : less_key(b, a))
-                               : (BY_PWR ? less_pwr(a, b) : less_key(a, b));
-          if (swap) {
-            keys[i] = b.key; pwrs[i] = b.pwr;
-            keys[ixj] = a.key; pwrs[ixj] = a.pwr;
-          }
-        }
-      }
-      __syncthreads();
-    }
-  }
+// "a is stronger than b": power descending, key ascending on ties
+__device__ __forceinline__ bool stronger(float pa, unsigned long long ka, float pb, unsigned long long kb) {
+  return pa > pb || (pa == pb && ka < kb);
 }
 
 __global__ void __launch_bounds__(1024) select_finalize_kernel(SelectParams p) {
   extern __shared__ __align__(16) unsigned char fz_smem[];
   const int plane = blockIdx.x;
-  const int n = (int)min(p.sel_count[plane], (unsigned)kSortCap);
-  int m = 1;
-  while (m < n) m <<= 1;
-  unsigned long long *keys = reinterpret_cast<unsigned long long *>(fz_smem);
-  float *pwrs = reinterpret_cast<float *>(keys + kSortCap);
-  const unsigned long long *gk = p.sel_key + (size_t)plane * kSortCap;
-  const float *gp = p.sel_pwr + (size_t)plane * kSortCap;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) {
-    keys[i] = i < n ? gk[i] : ~0ull;
-    pwrs[i] = i < n ? gp[i] : -CUDART_INF_F;
+  const int K = p.per_plane;
+  unsigned long long *bkey = reinterpret_cast<unsigned long long *>(fz_smem);  // [kSortCap] boundary
+  float *bpwr = reinterpret_cast<float *>(bkey + kSortCap);
+  unsigned long long *fin = reinterpret_cast<unsigned long long *>(bpwr + kSortCap);  // [kMaxCompat] kept
+  float *finp = reinterpret_cast<float *>(fin + kMaxCompat);
+  const int a = (int)min(p.sure_count[plane], (unsigned)kSortCap);
+  const int b = (int)min(p.bound_count[plane], (unsigned)kSortCap);
+  const size_t base = (size_t)plane * 2 * kSortCap;
+  // the sure records are all kept (fewer than K unless every hit was taken)
+  const int keep_a = min(a, K);
+  for (int i = threadIdx.x; i < keep_a; i += blockDim.x) {
+    fin[i] = p.sel_key[base + i];
+    finp[i] = p.sel_pwr[base + i];
+  }
+  for (int i = threadIdx.x; i < b; i += blockDim.x) {
+    bkey[i] = p.sel_key[base + kSortCap + i];
+    bpwr[i] = p.sel_pwr[base + kSortCap + i];
   }
   __syncthreads();
-  int kept = n;
-  if (n > p.per_plane) {
-    bitonic_sort<true>(keys, pwrs, m);
-    kept = p.per_plane;
-    for (int i = threadIdx.x; i < m; i += blockDim.x)
-      if (i >= kept) { keys[i] = ~0ull; pwrs[i] = -CUDART_INF_F; }
-    __syncthreads();
-  }
-  if (kept > 1) bitonic_sort<false>(keys, pwrs, m);
-  uint32_t *cl = p.compat_loc + (size_t)plane * p.per_plane;
-  float *cp = p.compat_pwr + (size_t)plane * p.per_plane;
-  for (int i = threadIdx.x; i < p.per_plane; i += blockDim.x) {
-    if (i < kept) {
-      const unsigned row = (unsigned)(keys[i] >> 32) & 0xffffu, bin = (unsigned)(keys[i] & 0xffffffffu);
-      // gen_info.h:62-64: ((h-1)&7)<<29 | (row&0x7f)<<22 | (bin&0x3fffff)
-      cl[i] = (((unsigned)plane & 7u) << 29) | ((row & 0x7fu) << 22) | (bin & 0x3fffffu);
-      cp[i] = pwrs[i];
-    } else {
-      cl[i] = p.invalid_location;
-      cp[i] = -1.0f;
+  // boundary records: rank among themselves, keep the c strongest
+  const int c = max(0, min(K - keep_a, b));
+  for (int i = threadIdx.x; i < b; i += blockDim.x) {
+    const unsigned long long ki = bkey[i];
+    const float pi = bpwr[i];
+    int rank = 0;
+    for (int j = 0; j < b; ++j) rank += stronger(bpwr[j], bkey[j], pi, ki);
+    if (rank < c) {
+      fin[keep_a + rank] = ki;
+      finp[keep_a + rank] = pi;
     }
+  }
+  __syncthreads();
+  const int kept = keep_a + c;
+  uint32_t *cl = p.compat_loc + (size_t)plane * K;
+  float *cp = p.compat_pwr + (size_t)plane * K;
+  // order the kept records by location: position = number of smaller keys
+  for (int i = threadIdx.x; i < kept; i += blockDim.x) {
+    const unsigned long long ki = fin[i];
+    int pos = 0;
+    for (int j = 0; j < kept; ++j) pos += fin[j] < ki;
+    const unsigned row = (unsigned)(ki >> 32) & 0xffffu, bin = (unsigned)(ki & 0xffffffffu);
+    // gen_info.h:62-64: ((h-1)&7)<<29 | (row&0x7f)<<22 | (bin&0x3fffff)
+    cl[pos] = (((unsigned)plane & 7u) << 29) | ((row & 0x7fu) << 22) | (bin & 0x3fffffu);
+    cp[pos] = finp[i];
+  }
+  for (int i = kept + threadIdx.x; i < K; i += blockDim.x) {
+    cl[i] = p.invalid_location;
+    cp[i] = -1.0f;
   }
 }
 
@@ -657,13 +633,22 @@ cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
 }
 
 cudaError_t launch_select(const SelectParams &p, cudaStream_t s) {
-  select_hist_kernel<<<4 * 152, 256, 0, s>>>(p);
-  select_threshold_kernel<<<p.n_planes, 1024, 0, s>>>(p);
-  select_gather_kernel<<<4 * 152, 256, 0, s>>>(p);
-  const int smem = kSortCap * (8 + 4);
-  cudaError_t e = cudaFuncSetAttribute(select_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  static int n_sm = 0;
+  if (!n_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (n_sm <= 0) n_sm = 1;
+  }
+  const int hsmem = p.n_planes * kSelBuckets * 4;
+  cudaError_t e = cudaFuncSetAttribute(select_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, hsmem);
   if (e != cudaSuccess) return e;
-  select_finalize_kernel<<<p.n_planes, 1024, smem, s>>>(p);
+  select_hist_kernel<<<n_sm, 1024, hsmem, s>>>(p);
+  select_gather_kernel<<<4 * n_sm, 256, 0, s>>>(p);
+  const int fsmem = (kSortCap + kMaxCompat) * (8 + 4);
+  e = cudaFuncSetAttribute(select_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, fsmem);
+  if (e != cudaSuccess) return e;
+  select_finalize_kernel<<<p.n_planes, 1024, fsmem, s>>>(p);
   return cudaGetLastError();
 }
 

@@ -235,7 +235,7 @@ void *fdas_get_stream(fdas_handle *h, fdas_buffer_set ab);
  * [0] status bits (1 staging timeout, 2 recheck list full, 4 candidate list
  * full, 8 selection buffer full, 16 FT-convolution timeout), [1] cells sent
  * to the FP64 recheck, [2] candidate records appended, [3 + p] hits of plane
- * p, [19 + p] records gathered for plane p's fixed-size list (p < 16). */
+ * p, [19 + p] hits of plane p certain to enter its fixed-size list (p < 16). */
 fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out, uint32_t n);
 
 /* Library version string. */
