@@ -209,9 +209,7 @@ __device__ __forceinline__ int srow(int r, int bh, int sgn) { return sgn > 0 ? r
 
 // Emission of plane j (0-based `plane`) straight from the accumulators: called
 // by the whole warp when some lane's tile reached the lower edge of the band.
-// Kept out of line: it runs rarely and would otherwise be inlined once per
-// plane, which blows the instruction cache of the hot loop.
-__device__ __noinline__ void emit_plane(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
+__device__ __forceinline__ void emit_plane(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
                                         const float (&acc)[4][4], int plane, int H, int sgn, int t0, int F) {
   const float hi = p.hi[plane], lo = p.lo[plane];
 #pragma unroll
@@ -329,8 +327,8 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_con
           for (int e = 0; e < 4; ++e)
             if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
       }
-      if (__any_sync(0xffffffffu, max16(acc) >= p.trig[0]))
-        emit_plane(eb, warp, wcount, p, acc, 0, H, sgn, t0, F);
+      // bit j-1: some lane of the warp reached the band of plane j (warp-uniform)
+      unsigned trig = __any_sync(0xffffffffu, max16(acc) >= p.trig[0]) ? 1u : 0u;
       hs_sfor<MAXP - 1>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value + 2;
         if (j <= P) {
@@ -379,11 +377,49 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_con
               }
             }
           }
-          // rare: some lane of the warp reached the band of plane j
-          if (__any_sync(0xffffffffu, max16(acc) >= p.trig[j - 1]))
-            emit_plane(eb, warp, wcount, p, acc, j - 1, H, sgn, t0, F);
+          if (__any_sync(0xffffffffu, max16(acc) >= p.trig[j - 1])) trig |= 1u << (j - 1);
         }
       });
+
+      // ---- rare: recompute the sums plane by plane (same values, same order)
+      // with the generic 2 x 2 window, which holds for every j >= 2, and emit
+      // the planes whose band was reached
+      if (trig) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const float4 q = *reinterpret_cast<const float4 *>(stage + p.soff[1] + srow(t0 + kk, kRows1, sgn) * kHsBins +
+                                                             4 * lane);
+          acc[kk][0] = q.x; acc[kk][1] = q.y; acc[kk][2] = q.z; acc[kk][3] = q.w;
+          if (!rowok[kk]) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = -CUDART_INF_F;
+        }
+        if (f0 + kHsBins > p.n_bins) {
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
+        }
+#pragma unroll 1
+        for (int j = 1; j <= P; ++j) {
+          if (j > 1) {
+            const int a0 = (f0 / j) & ~3;
+            const int bw = p.bw[j], bh = p.bh[j];
+            const int rb = t0 / j;
+            const int kstar = j - (t0 - rb * j);
+            const int bb = F / j;
+            const int estar = j - (F - bb * j);
+            const float *r0 = stage + p.soff[j] + (bb - a0) + srow(rb, bh, sgn) * bw;
+            const int rstep = sgn * bw;
+            const float v00 = r0[0], v01 = r0[1], v10 = r0[rstep], v11 = r0[rstep + 1];
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+              for (int e = 0; e < 4; ++e)
+                acc[kk][e] += kk < kstar ? (e < estar ? v00 : v01) : (e < estar ? v10 : v11);
+          }
+          if ((trig >> (j - 1)) & 1u) emit_plane(eb, warp, wcount, p, acc, j - 1, H, sgn, t0, F);
+        }
+      }
 
       // release the stage to the producer
       __syncwarp();
