@@ -35,6 +35,7 @@ class FdasConfig(ctypes.Structure):
         ("sync_pipeline", ctypes.c_uint32),
         ("recheck", ctypes.c_uint32),
         ("recheck_band", ctypes.c_float),
+        ("overlap", ctypes.c_uint32),
     ]
 
 

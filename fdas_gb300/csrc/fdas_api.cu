@@ -272,6 +272,7 @@ fdas_status enqueue_ftc(fdas_handle *h, int ab, fdas_fop_part which) {
   p.twiddle = h->d_twiddle;
   p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlStatus);
   p.timeout_ns = 2000000000LL;  // 2 s
+  p.ctas_per_sm = h->cfg.overlap ? 1 : 2;
   CK(h, launch_ftc(p, S.stream));
   CK(h, cudaEventRecord(S.ev[3], S.stream));
   S.ev_ftc_recorded = true;
@@ -315,6 +316,7 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   }
   hsum_geometry(h, p);
   p.item_counter = S.d_ctrl + kCtrlItems;
+  p.lean = h->cfg.overlap && P <= 8 && hsum_warps(H) == 11 ? 1 : 0;
   p.cand_key = S.d_key;
   p.cand_pwr = S.d_pwr;
   p.cand_total = S.d_ctrl + kCtrlTotal;

@@ -55,6 +55,7 @@ struct FtcParams {
   const float2 *twiddle;
   int *status;
   long long timeout_ns;
+  int ctas_per_sm;        // persistent CTAs per SM (1 leaves room for harmonic summing)
 };
 
 // ---- (d) harmonic summing + thresholds + candidate compaction (preload,
@@ -87,6 +88,7 @@ struct HsumParams {
   int rc_cap;
   int *status;
   long long timeout_ns;   // bound on every wait
+  int lean;               // 1: 3 stages and <= 80 registers (shares an SM with the FT convolution)
 };
 
 // 2-D tensor maps of the FOP (rows x stride floats), one box shape per plane

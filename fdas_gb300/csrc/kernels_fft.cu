@@ -327,7 +327,8 @@ cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
     cudaError_t e = cudaFuncSetAttribute(ftc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     const long long ctas = (items + kPairsPerCta - 1) / kPairsPerCta;
-    ftc2_kernel<<<(int)(ctas < 2 * n_sm ? ctas : 2 * n_sm), 256, smem, s>>>(p);
+    const long long per_sm = p.ctas_per_sm >= 1 && p.ctas_per_sm <= 2 ? p.ctas_per_sm : 2;
+    ftc2_kernel<<<(int)(ctas < per_sm * n_sm ? ctas : per_sm * n_sm), 256, smem, s>>>(p);
   }
   return cudaGetLastError();
 }

@@ -227,9 +227,9 @@ __device__ __forceinline__ void emit_plane(EmitBuf &eb, int warp, unsigned &wcou
   }
 }
 
-template <int MAXP, int NW, int kHsStages>
-__global__ void __launch_bounds__(32 * (NW + 1), 1) hsum_kernel(const __grid_constant__ HsumParams p,
-                                                                 const __grid_constant__ HsumMaps m) {
+template <int MAXP, int NW, int kHsStages, int MINB>
+__global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_constant__ HsumParams p,
+                                                                    const __grid_constant__ HsumMaps m) {
   extern __shared__ __align__(1024) float hs_smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(hs_smem);  // [kHsStages]
   uint64_t *empty = full + kHsStages;                        // [kHsStages]
@@ -631,17 +631,20 @@ __global__ void __launch_bounds__(1024) select_finalize_kernel(SelectParams p) {
 
 // ----------------------------------------------------------------- launchers
 int hsum_warps(int half) { return (half + 1 + 3) / 4 <= 11 ? 11 : 16; }
-static int hsum_stages(int half) { return hsum_warps(half) == 11 ? 4 : 3; }
-
-int hsum_smem_bytes(const HsumParams &p) {
-  return 1024 + hsum_stages(p.half) * p.stage_floats * 4 + (int)sizeof(EmitBuf);
+static int hsum_stages(const HsumParams &p) {
+  if (p.lean) return 3;
+  return hsum_warps(p.half) == 11 ? 4 : 3;
 }
 
-template <int MAXP, int NW, int STAGES>
+int hsum_smem_bytes(const HsumParams &p) {
+  return 1024 + hsum_stages(p) * p.stage_floats * 4 + (int)sizeof(EmitBuf);
+}
+
+template <int MAXP, int NW, int STAGES, int MINB>
 static cudaError_t launch_hsum_t(const HsumParams &p, const HsumMaps &m, cudaStream_t s) {
   const int smem = hsum_smem_bytes(p);
   cudaError_t e =
-      cudaFuncSetAttribute(hsum_kernel<MAXP, NW, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      cudaFuncSetAttribute(hsum_kernel<MAXP, NW, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   static int n_sm = 0;
   if (!n_sm) {
@@ -651,16 +654,20 @@ static cudaError_t launch_hsum_t(const HsumParams &p, const HsumMaps &m, cudaStr
     if (n_sm <= 0) n_sm = 1;
   }
   const int items = (p.n_bins + kHsBins - 1) / kHsBins * 2;
-  hsum_kernel<MAXP, NW, STAGES><<<items < n_sm ? items : n_sm, 32 * (NW + 1), smem, s>>>(p, m);
+  hsum_kernel<MAXP, NW, STAGES, MINB><<<items < n_sm ? items : n_sm, 32 * (NW + 1), smem, s>>>(p, m);
   return cudaGetLastError();
 }
 
 cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s) {
   if (hsum_warps(p.half) == 11) {
-    if (p.n_planes <= 8) return launch_hsum_t<8, 11, 4>(p, m, s);
-    return launch_hsum_t<16, 11, 4>(p, m, s);
+    if (p.n_planes <= 8) {
+      // lean: 3 stages and a register budget that fits next to one FT-convolution CTA
+      if (p.lean) return launch_hsum_t<8, 11, 3, 2>(p, m, s);
+      return launch_hsum_t<8, 11, 4, 1>(p, m, s);
+    }
+    return launch_hsum_t<16, 11, 4, 1>(p, m, s);
   }
-  return launch_hsum_t<16, 16, 3>(p, m, s);
+  return launch_hsum_t<16, 16, 3, 1>(p, m, s);
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {

@@ -95,6 +95,9 @@ typedef struct {
   uint32_t sync_pipeline;      /* FDAS::initialise_accelerator sync_pipeline */
   uint32_t recheck;            /* 1 = FP64 recheck of near-threshold cells (default) */
   float recheck_band;          /* relative band around each threshold; 0 = 1e-4 */
+  uint32_t overlap;            /* 1 = size the kernels so that the FT convolution of one
+                                  buffer set and the harmonic summing of the other run
+                                  concurrently on every SM (for pipelined A/B searches) */
 } fdas_config;
 
 /* Fill `cfg` with the reference's defaults for `n_frequency_bins` bins. */
