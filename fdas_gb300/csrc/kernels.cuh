@@ -9,7 +9,7 @@ namespace fdas {
 
 constexpr int kTile = 2048;          // FFT / tile size (gen_info.h:33, 42)
 constexpr int kMaxPlanes = 16;       // harmonic planes supported by the kernels
-constexpr int kHsBins = 128;         // bins per harmonic-summing work item
+constexpr int kHsBins = 256;         // bins per harmonic-summing work item
 constexpr int kSortCap = 8192;       // boundary records one CTA ranks in shared memory
 constexpr int kMaxCompat = 2048;     // entries per plane of the fixed-size list
 constexpr int kEmitBuf = 1024;       // candidate records staged per harmonic-summing CTA

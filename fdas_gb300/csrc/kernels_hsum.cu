@@ -71,7 +71,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, long long timeo
 // Candidate staging: each warp collects its records in a shared-memory
 // buffer (warp ballot -> one slot range per batch) and moves a full buffer to
 // the global list with a single atomic reservation.
-constexpr int kWarpBuf = 64;
+constexpr int kWarpBuf = 32;
 constexpr int kHsMaxWarps = 16;  // templates per half <= 64
 
 struct EmitBuf {
@@ -137,28 +137,29 @@ __device__ __forceinline__ void warp_recheck(const HsumParams &p, unsigned nm, i
   }
 }
 
-// Persistent harmonic summing.  Work item = (128-bin block, sign half),
+// Persistent harmonic summing.  Work item = (256-bin block, sign half),
 // handed out dynamically through a global counter.  A CTA has NW consumer
 // warps -- warp w owns templates |t| = 4w + k (k < 4), lane l the bins
-// f0 + 4 l + e (e < 4), i.e. a 4 x 4 tile of cells aligned to 4 in both
-// directions -- and one producer warp.  For every item the producer issues one
-// 2-D TMA tensor copy per plane (cp.async.bulk.tensor.2d): plane 1 as 128 bins
-// x 4 NW rows, plane j >= 2 as the rows trunc(t/j) of the half over bins
-// [(f0/j) & ~3, ...); rows and bins outside the FOP are zero-filled by the
-// hardware (they only feed masked cells).  kHsStages stages deep: full /
-// empty mbarriers, every wait bounded by %globaltimer.
+// f0 + 8 l + e (e < 8), i.e. a 4 x 8 tile of cells aligned to 4 and 8 -- and
+// one producer warp.  For every item the producer issues one 2-D TMA tensor
+// copy per plane (cp.async.bulk.tensor.2d): plane 1 as 256 bins x 4 NW rows,
+// plane j >= 2 as the rows trunc(t/j) of the half over bins [(f0/j) & ~3, ...);
+// rows and bins outside the FOP are zero-filled by the hardware (they only
+// feed masked cells).  kHsStages stages deep: full / empty mbarriers, every
+// wait bounded by %globaltimer.
 //
-// With the tile aligned to 4, planes 2, 4 and 8 map the 16 cells onto 2 x 2,
-// 1 and 1 staged values at compile-time offsets; planes 3, 5, 6, 7 onto a
-// 2 x 2 window whose split points are computed once per item.
+// With the tile aligned, planes 2, 4 and 8 read their values with 16-, 8- and
+// 4-byte loads at compile-time offsets; for planes 3, 5, 6, 7 the eight bins
+// map onto per-bin offsets computed once per item and the four rows onto two
+// staged rows split at a warp-uniform point, handled by a switch.
 //
 // HP_1 = FOP[t][f], HP_j = HP_{j-1} + FOP[trunc(t/j)][f/j] accumulated in FP32
 // in this order -- hsum.py:95-120 / hms_baseline.cl.mako:55-84 -- so the
 // values match hsum.py bit for bit for the same FOP.  A cell is a candidate of
 // plane j if HP_j > thr_j (strict, hsum.py:134 / detect.cl.mako:185).  The fast
-// path keeps one flag per thread (max over the 16 cells per plane against the
-// lower edge of the plane's band); flagged warps re-walk their cells
-// warp-synchronously and emit through ballots.
+// path only takes the maximum of the tile per plane; if some lane of the warp
+// reaches the lower edge of a plane's band, the warp recomputes its sums plane
+// by plane and emits through ballots.
 struct HsItem {
   int f0, sgn, tlo;
 };
@@ -177,12 +178,18 @@ __device__ __forceinline__ int hs_n_items(const HsumParams &p) {
   return nb * ((p.tlo[0] <= p.half) + (p.tlo[1] <= p.half));
 }
 
-__device__ __forceinline__ float max16(const float (&a)[4][4]) {
-  float m0 = fmaxf(fmaxf(a[0][0], a[0][1]), fmaxf(a[0][2], a[0][3]));
-  float m1 = fmaxf(fmaxf(a[1][0], a[1][1]), fmaxf(a[1][2], a[1][3]));
-  float m2 = fmaxf(fmaxf(a[2][0], a[2][1]), fmaxf(a[2][2], a[2][3]));
-  float m3 = fmaxf(fmaxf(a[3][0], a[3][1]), fmaxf(a[3][2], a[3][3]));
-  return fmaxf(fmaxf(m0, m1), fmaxf(m2, m3));
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+// maximum of the 32 cells of a tile (3-input max tree)
+__device__ __forceinline__ float max32(const float (&a)[4][8]) {
+  float m[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    m[k] = fmax3(fmax3(a[k][0], a[k][1], a[k][2]), fmax3(a[k][3], a[k][4], a[k][5]), fmaxf(a[k][6], a[k][7]));
+  return fmax3(m[0], m[1], fmaxf(m[2], m[3]));
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -207,15 +214,45 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
 // boxes hold FOP rows in ascending order, i.e. reversed for the negative half
 __device__ __forceinline__ int srow(int r, int bh, int sgn) { return sgn > 0 ? r : bh - 1 - r; }
 
-// Emission of plane j (0-based `plane`) straight from the accumulators: called
-// by the whole warp when some lane's tile reached the lower edge of the band.
+// acc[k][e] += (k < KS ? c0[e] : c1[e]), KS compile time
+template <int KS>
+__device__ __forceinline__ void add_rows(float (&acc)[4][8], const float (&c0)[8], const float (&c1)[8]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[k][e] += k < KS ? c0[e] : c1[e];
+}
+
+// plane j >= 2 added to the tile, generic form (any j, runtime)
+__device__ __forceinline__ void add_plane_generic(float (&acc)[4][8], const float *stage, const HsumParams &p, int j,
+                                                  int f0, int t0, int F, int sgn) {
+  const int a0 = (f0 / j) & ~3;
+  const int bw = p.bw[j], bh = p.bh[j];
+  const int rb = t0 / j;
+  const int kstar = j - (t0 - rb * j);
+  const float *r0 = stage + p.soff[j] + srow(rb, bh, sgn) * bw - a0;
+  const float *r1 = r0 + sgn * bw;
+  float c0[8], c1[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int o = (F + e) / j;
+    c0[e] = r0[o];
+    c1[e] = r1[o];
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[k][e] += k < kstar ? c0[e] : c1[e];
+}
+
+// Emission of plane `plane` (0-based) from the accumulators; whole warp.
 __device__ __forceinline__ void emit_plane(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
-                                        const float (&acc)[4][4], int plane, int H, int sgn, int t0, int F) {
+                                           const float (&acc)[4][8], int plane, int H, int sgn, int t0, int F) {
   const float hi = p.hi[plane], lo = p.lo[plane];
 #pragma unroll
   for (int kk = 0; kk < 4; ++kk) {
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
+    for (int e = 0; e < 8; ++e) {
       const float a = acc[kk][e];  // -inf for masked cells
       const bool hit = a > hi;
       const bool near = !hit && a >= lo;
@@ -257,7 +294,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
     if (lane == 0) {
       // items are taken from the global counter in chunks of kChunk, and the
       // next chunk is requested one chunk ahead so the atomic's latency is hidden
-      constexpr int kChunk = 4;
+      constexpr int kChunk = 2;
       int cur = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
       int nxt = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
       int used = 0;
@@ -306,117 +343,97 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
       const HsItem item = hs_item(p, it);
       const int f0 = item.f0, sgn = item.sgn;
       const float *stage = stages + st * p.stage_floats;
-      const int F = f0 + 4 * lane;
+      const int Fl = 8 * lane;  // first bin of the tile within the block
+      const int F = f0 + Fl;
       bool rowok[4];
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk) rowok[kk] = (t0 + kk <= H) && (t0 + kk >= item.tlo);
-      float acc[4][4];
-      {
-        const float *r1 = stage + p.soff[1] + 4 * lane;
+      const bool tail = f0 + kHsBins > p.n_bins;
+      float acc[4][8];
+      auto load_plane1 = [&]() {
+        const float *r1 = stage + p.soff[1] + Fl;
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) {
-          const float4 q = *reinterpret_cast<const float4 *>(r1 + srow(t0 + kk, kRows1, sgn) * kHsBins);
-          acc[kk][0] = q.x; acc[kk][1] = q.y; acc[kk][2] = q.z; acc[kk][3] = q.w;
-          if (!rowok[kk]) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = -CUDART_INF_F;
+          const float *rr = r1 + srow(t0 + kk, kRows1, sgn) * kHsBins;
+          const float4 q0 = *reinterpret_cast<const float4 *>(rr);
+          const float4 q1 = *reinterpret_cast<const float4 *>(rr + 4);
+          acc[kk][0] = q0.x; acc[kk][1] = q0.y; acc[kk][2] = q0.z; acc[kk][3] = q0.w;
+          acc[kk][4] = q1.x; acc[kk][5] = q1.y; acc[kk][6] = q1.z; acc[kk][7] = q1.w;
+          if (!rowok[kk]) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) acc[kk][e] = -CUDART_INF_F;
+          }
         }
-      }
-      if (f0 + kHsBins > p.n_bins) {
+        if (tail) {
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
+          for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-          for (int e = 0; e < 4; ++e)
-            if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
-      }
+            for (int e = 0; e < 8; ++e)
+              if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
+        }
+      };
+      load_plane1();
       // bit j-1: some lane of the warp reached the band of plane j (warp-uniform)
-      unsigned trig = __any_sync(0xffffffffu, max16(acc) >= p.trig[0]) ? 1u : 0u;
+      unsigned trig = __any_sync(0xffffffffu, max32(acc) >= p.trig[0]) ? 1u : 0u;
       hs_sfor<MAXP - 1>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value + 2;
         if (j <= P) {
           const int a0 = (f0 / j) & ~3;
           const int bw = p.bw[j], bh = p.bh[j];
           const float *box = stage + p.soff[j];
-          const int rstep = sgn * bw;  // smem distance of staged rows r and r + 1
-          if constexpr (j == 2 || j == 4 || j == 8) {
-            const float *blk = box + (F / j - a0) + srow(t0 / j, bh, sgn) * bw;
-            if constexpr (j == 2) {
-              const float2 r0 = *reinterpret_cast<const float2 *>(blk);
-              const float2 r1 = *reinterpret_cast<const float2 *>(blk + rstep);
-#pragma unroll
-              for (int kk = 0; kk < 4; ++kk) {
-                const float2 r = kk < 2 ? r0 : r1;
-                acc[kk][0] += r.x; acc[kk][1] += r.x; acc[kk][2] += r.y; acc[kk][3] += r.y;
-              }
-            } else {
-              const float v = *blk;
-#pragma unroll
-              for (int kk = 0; kk < 4; ++kk)
-#pragma unroll
-                for (int e = 0; e < 4; ++e) acc[kk][e] += v;
-            }
-          } else {
-            const int rb = t0 / j;
-            const int kstar = j - (t0 - rb * j);  // first k with trunc((t0+k)/j) = rb + 1
-            const int bb = F / j;
-            const int estar = j - (F - bb * j);   // first e with (F+e)/j = bb + 1
-            const float *r0 = box + (bb - a0) + srow(rb, bh, sgn) * bw;
-            const float v00 = r0[0], v01 = r0[1], v10 = r0[rstep], v11 = r0[rstep + 1];
-            float c0[4], c1[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              c0[e] = e < estar ? v00 : v01;
-              c1[e] = e < estar ? v10 : v11;
-            }
+          if constexpr (j == 2) {
+            const float *r0 = box + srow(t0 / 2, bh, sgn) * bw + (F / 2 - a0);
+            const float4 v0 = *reinterpret_cast<const float4 *>(r0);
+            const float4 v1 = *reinterpret_cast<const float4 *>(r0 + sgn * bw);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
-              if (kk < kstar) {  // warp-uniform
+              const float4 v = kk < 2 ? v0 : v1;
+              acc[kk][0] += v.x; acc[kk][1] += v.x; acc[kk][2] += v.y; acc[kk][3] += v.y;
+              acc[kk][4] += v.z; acc[kk][5] += v.z; acc[kk][6] += v.w; acc[kk][7] += v.w;
+            }
+          } else if constexpr (j == 4) {
+            const float2 v = *reinterpret_cast<const float2 *>(box + srow(t0 / 4, bh, sgn) * bw + (F / 4 - a0));
 #pragma unroll
-                for (int e = 0; e < 4; ++e) acc[kk][e] += c0[e];
-              } else {
+            for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-                for (int e = 0; e < 4; ++e) acc[kk][e] += c1[e];
-              }
+              for (int e = 0; e < 8; ++e) acc[kk][e] += e < 4 ? v.x : v.y;
+          } else if constexpr (j == 8) {
+            const float v = box[srow(t0 / 8, bh, sgn) * bw + (F / 8 - a0)];
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+              for (int e = 0; e < 8; ++e) acc[kk][e] += v;
+          } else {
+            const int rb = t0 / j;
+            const int kstar = j - (t0 - rb * j);  // warp-uniform: first k with trunc((t0+k)/j) = rb + 1
+            const float *r0 = box + srow(rb, bh, sgn) * bw - a0;
+            const float *r1 = r0 + sgn * bw;
+            float c0[8], c1[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+              const int o = (F + e) / j;
+              c0[e] = r0[o];
+              c1[e] = r1[o];
+            }
+            switch (kstar < 4 ? kstar : 4) {
+              case 1: add_rows<1>(acc, c0, c1); break;
+              case 2: add_rows<2>(acc, c0, c1); break;
+              case 3: add_rows<3>(acc, c0, c1); break;
+              default: add_rows<4>(acc, c0, c1); break;
             }
           }
-          if (__any_sync(0xffffffffu, max16(acc) >= p.trig[j - 1])) trig |= 1u << (j - 1);
+          if (__any_sync(0xffffffffu, max32(acc) >= p.trig[j - 1])) trig |= 1u << (j - 1);
         }
       });
 
       // ---- rare: recompute the sums plane by plane (same values, same order)
-      // with the generic 2 x 2 window, which holds for every j >= 2, and emit
-      // the planes whose band was reached
+      // and emit the planes whose band was reached
       if (trig) {
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const float4 q = *reinterpret_cast<const float4 *>(stage + p.soff[1] + srow(t0 + kk, kRows1, sgn) * kHsBins +
-                                                             4 * lane);
-          acc[kk][0] = q.x; acc[kk][1] = q.y; acc[kk][2] = q.z; acc[kk][3] = q.w;
-          if (!rowok[kk]) acc[kk][0] = acc[kk][1] = acc[kk][2] = acc[kk][3] = -CUDART_INF_F;
-        }
-        if (f0 + kHsBins > p.n_bins) {
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-#pragma unroll
-            for (int e = 0; e < 4; ++e)
-              if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
-        }
+        load_plane1();
+        const int last = 32 - __clz(trig);  // highest plane needed
 #pragma unroll 1
-        for (int j = 1; j <= P; ++j) {
-          if (j > 1) {
-            const int a0 = (f0 / j) & ~3;
-            const int bw = p.bw[j], bh = p.bh[j];
-            const int rb = t0 / j;
-            const int kstar = j - (t0 - rb * j);
-            const int bb = F / j;
-            const int estar = j - (F - bb * j);
-            const float *r0 = stage + p.soff[j] + (bb - a0) + srow(rb, bh, sgn) * bw;
-            const int rstep = sgn * bw;
-            const float v00 = r0[0], v01 = r0[1], v10 = r0[rstep], v11 = r0[rstep + 1];
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk)
-#pragma unroll
-              for (int e = 0; e < 4; ++e)
-                acc[kk][e] += kk < kstar ? (e < estar ? v00 : v01) : (e < estar ? v10 : v11);
-          }
+        for (int j = 1; j <= last; ++j) {
+          if (j > 1) add_plane_generic(acc, stage, p, j, f0, t0, F, sgn);
           if ((trig >> (j - 1)) & 1u) emit_plane(eb, warp, wcount, p, acc, j - 1, H, sgn, t0, F);
         }
       }
@@ -632,8 +649,7 @@ __global__ void __launch_bounds__(1024) select_finalize_kernel(SelectParams p) {
 // ----------------------------------------------------------------- launchers
 int hsum_warps(int half) { return (half + 1 + 3) / 4 <= 11 ? 11 : 16; }
 static int hsum_stages(const HsumParams &p) {
-  if (p.lean) return 3;
-  return hsum_warps(p.half) == 11 ? 4 : 3;
+  return (p.lean || p.n_planes > 8 || hsum_warps(p.half) != 11) ? 2 : 3;
 }
 
 int hsum_smem_bytes(const HsumParams &p) {
@@ -661,13 +677,13 @@ static cudaError_t launch_hsum_t(const HsumParams &p, const HsumMaps &m, cudaStr
 cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s) {
   if (hsum_warps(p.half) == 11) {
     if (p.n_planes <= 8) {
-      // lean: 3 stages and a register budget that fits next to one FT-convolution CTA
-      if (p.lean) return launch_hsum_t<8, 11, 3, 2>(p, m, s);
-      return launch_hsum_t<8, 11, 4, 1>(p, m, s);
+      // lean: 2 stages and a register budget that fits next to one FT-convolution CTA
+      if (p.lean) return launch_hsum_t<8, 11, 2, 2>(p, m, s);
+      return launch_hsum_t<8, 11, 3, 1>(p, m, s);
     }
-    return launch_hsum_t<16, 11, 4, 1>(p, m, s);
+    return launch_hsum_t<16, 11, 2, 1>(p, m, s);
   }
-  return launch_hsum_t<16, 16, 3, 1>(p, m, s);
+  return launch_hsum_t<16, 16, 2, 1>(p, m, s);
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
