@@ -88,6 +88,7 @@ SIGNATURES = {
     "fdas_synchronize": (_INT, [_P, _INT]),
     "fdas_get_stream": (_P, [_P, _INT]),
     "fdas_get_counters": (_INT, [_P, _INT, _P, _U32]),
+    "fdas_retrieve_candidates_ring": (_INT, [_P, _P, _P, _INT, _INT]),
     "fdas_version": (ctypes.c_char_p, []),
 }
 

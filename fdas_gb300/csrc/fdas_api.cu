@@ -894,6 +894,75 @@ fdas_status fdas_retrieve_candidate_list(fdas_handle *h, fdas_candidate *out, ui
   return FDAS_OK;
 }
 
+fdas_status fdas_retrieve_candidates_ring(fdas_handle *h, uint32_t *detection_location, float *detection_power,
+                                          fdas_fop_part which, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!detection_location || !detection_power) return fail(h, FDAS_ERR_INVALID_ARG, "output is NULL");
+  if (which != FDAS_NEGATIVE_ACCELERATIONS && which != FDAS_POSITIVE_ACCELERATIONS)
+    return fail(h, FDAS_ERR_UNSUPPORTED, "the FPGA candidate ring covers one sign half (FDAS.cpp:447-450)");
+  CK(h, cudaSetDevice(h->cfg.device));
+  fdas_status st = sync_set(h, ab);
+  if (st != FDAS_OK) return st;
+  BufferSet &S = h->set[ab];
+  unsigned ctrl[kCtrlWords];
+  CK(h, cudaMemcpy(ctrl, S.d_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
+  const uint32_t stored = std::min(ctrl[kCtrlTotal], (unsigned)h->cap);
+  std::vector<unsigned long long> keys(stored);
+  std::vector<float> pwrs(stored);
+  if (stored) {
+    CK(h, cudaMemcpy(keys.data(), S.d_key, sizeof(unsigned long long) * stored, cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpy(pwrs.data(), S.d_pwr, sizeof(float) * stored, cudaMemcpyDeviceToHost));
+  }
+  // FPGA geometry of the shipped design: groups of 4 templates, bundles of 2
+  // bins, 64 slots of 8 lanes per plane (gen_info.h:47-54)
+  constexpr int kGroup = 4, kBundle = 2, kSlots = 64, kLanes = 8;
+  const uint32_t invalid = (uint32_t)((h->H + 1 + h->H) & 0x7f) << 22;
+  const size_t n_out = (size_t)h->P * kSlots * kLanes;
+  for (size_t i = 0; i < n_out; ++i) {
+    detection_location[i] = invalid;
+    detection_power[i] = -1.0f;
+  }
+  struct Hit {
+    unsigned long long ev;  // scan order: group-major, then bundle
+    int lane;
+    uint32_t loc;
+    float pwr;
+  };
+  std::vector<std::vector<Hit>> per_plane(h->P);
+  for (uint32_t i = 0; i < stored; ++i) {
+    const int plane = (int)(keys[i] >> 48);
+    const int row = (int)((keys[i] >> 32) & 0xffffu);
+    const uint32_t bin = (uint32_t)(keys[i] & 0xffffffffu);
+    const int t = row - h->H;
+    if ((which == FDAS_NEGATIVE_ACCELERATIONS && t > 0) || (which == FDAS_POSITIVE_ACCELERATIONS && t < 0)) continue;
+    const int at = t < 0 ? -t : t;
+    Hit x;
+    x.ev = ((unsigned long long)(at / kGroup) << 32) | (bin / kBundle);
+    x.lane = (at % kGroup) * kBundle + (int)(bin % kBundle);
+    x.loc = (((unsigned)plane & 7u) << 29) | (((unsigned)row & 0x7fu) << 22) | (bin & 0x3fffffu);
+    x.pwr = pwrs[i];
+    per_plane[plane].push_back(x);
+  }
+  for (int pl = 0; pl < h->P; ++pl) {
+    auto &v = per_plane[pl];
+    std::sort(v.begin(), v.end(), [](const Hit &a, const Hit &b) { return a.ev < b.ev || (a.ev == b.ev && a.lane < b.lane); });
+    // events in scan order; the last kSlots survive, slot = event index mod kSlots
+    size_t n_ev = 0;
+    for (size_t i = 0; i < v.size(); ++i)
+      if (i == 0 || v[i].ev != v[i - 1].ev) ++n_ev;
+    size_t rank = 0;
+    for (size_t i = 0; i < v.size(); ++i) {
+      if (i > 0 && v[i].ev != v[i - 1].ev) ++rank;
+      if (rank + kSlots < n_ev) continue;
+      const size_t o = ((size_t)pl * kSlots + rank % kSlots) * kLanes + v[i].lane;
+      detection_location[o] = v[i].loc;
+      detection_power[o] = v[i].pwr;
+    }
+  }
+  return FDAS_OK;
+}
+
 fdas_status fdas_get_stage_times(fdas_handle *h, fdas_buffer_set ab, float *ms6) {
   CHECK_HANDLE(h);
   CHECK_SET(h, ab);

@@ -227,6 +227,15 @@ class FDAS:
         kept = min(int(n_total.value) - int(n_dropped.value), capacity)
         return out[:kept], int(n_total.value), int(n_dropped.value)
 
+    def retrieve_candidates_ring(self, detection_location, detection_power, which, ab):
+        """The FPGA's 64-slot candidate ring of one sign half, reproduced from
+        the hits (for side-by-side comparison with FPGA logs)."""
+        n = self.config.n_planes * 64 * 8
+        loc = _require(detection_location, np.uint32, n, "detection_location")
+        pwr = _require(detection_power, np.float32, n, "detection_power")
+        return self._check(self._lib.fdas_retrieve_candidates_ring(self._h, _ptr(loc), _ptr(pwr), int(which), int(ab)),
+                           "retrieve_candidates_ring")
+
     def counters(self, ab):
         """Device counters of the last harmonic summing: dict with status,
         recheck (cells sent to the FP64 recheck), records and per-plane hits."""

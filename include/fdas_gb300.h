@@ -191,6 +191,17 @@ typedef struct {
 fdas_status fdas_retrieve_candidate_list(fdas_handle *h, fdas_candidate *out, uint32_t capacity,
                                          uint32_t *n_total, uint32_t *n_dropped, fdas_buffer_set ab);
 
+/* The reference FPGA's own candidate list for one sign half (which =
+ * FDAS_NEGATIVE_ACCELERATIONS or FDAS_POSITIVE_ACCELERATIONS), reproduced from
+ * the hits of the last harmonic summing on `ab`: per plane a 64-slot ring of
+ * 8-lane events, scanned in template groups of 4 and bin bundles of 2, where
+ * later events overwrite older ones (detect.cl.mako:32-216, store_cands.cl.mako:
+ * 21-33).  n_planes x 64 x 8 entries, [plane][slot][lane]; empty entries hold
+ * location encode(1, 43, 0) and power -1.  For side-by-side comparison with
+ * FPGA logs.  Blocking. */
+fdas_status fdas_retrieve_candidates_ring(fdas_handle *h, uint32_t *detection_location, float *detection_power,
+                                          fdas_fop_part which, fdas_buffer_set ab);
+
 /* FDAS::print_stats / print_events (FDAS.h:75-77, FDAS.cpp:643-686): write the
  * stage timings of the last launch on `ab` to the log (stderr by default). */
 void fdas_print_stats(fdas_handle *h, fdas_buffer_set ab, int reset);

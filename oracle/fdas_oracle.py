@@ -365,3 +365,38 @@ def harmonic_planes_streaming_error(fop32, fop64, thresholds, n_planes=8, window
         if sel.any():
             worst = max(worst, float(np.max(np.abs(h32[sel].astype(np.float64) - h64[sel])) / thr))
     return worst
+
+
+def ring_list(loc, pwr, part, n_planes=8, group_sz=4, bundle_sz=2, detection_sz=64):
+    """The FPGA detectors' candidate ring, reproduced from a hit list.
+
+    detect.cl.mako:141-216 scans one sign half in template groups of
+    ``group_sz`` (|t| = group_sz*g + p) and bins in bundles of ``bundle_sz``
+    (f = bundle_sz*b + q), group-major; every (g, b) with at least one hit is
+    an event written to slot ``next`` (next = (next + 1) mod detection_sz) with
+    lane p*bundle_sz + q.  Older events are overwritten, so the last
+    ``detection_sz`` events survive.  store_cands.cl.mako:21-33 emits plane-major
+    [plane][slot][lane] (the drain of detect.cl.mako:220-243); empty lanes and
+    slots hold (INVALID_LOCATION, -1).  ``part``: 'neg' or 'pos'.
+    """
+    slot_sz = 1 << int(np.ceil(np.log2(group_sz * bundle_sz)))
+    out_loc = np.full((n_planes, detection_sz, slot_sz), INVALID_LOCATION, dtype=np.uint32)
+    out_pwr = np.full((n_planes, detection_sz, slot_sz), INVALID_POWER, dtype=np.float32)
+    h, t, f = decode_location(loc)
+    sel = (t <= 0) if part == 'neg' else (t >= 0)
+    for k in range(1, n_planes + 1):
+        m = sel & (h == k)
+        if not m.any():
+            continue
+        tt, ff, ll, pp = np.abs(t[m]), f[m], np.asarray(loc)[m], np.asarray(pwr, dtype=np.float32)[m]
+        g, p = tt // group_sz, tt % group_sz
+        b, q = ff // bundle_sz, ff % bundle_sz
+        ev = g.astype(np.int64) * (int(ff.max()) // bundle_sz + 2) + b  # scan order
+        uniq, rank = np.unique(ev, return_inverse=True)
+        n_ev = uniq.size
+        keep = rank >= n_ev - detection_sz
+        slot = rank[keep] % detection_sz
+        lane = (p * bundle_sz + q)[keep]
+        out_loc[k - 1, slot, lane] = ll[keep]
+        out_pwr[k - 1, slot, lane] = pp[keep]
+    return out_loc.reshape(-1), out_pwr.reshape(-1)

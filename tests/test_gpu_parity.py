@@ -334,3 +334,23 @@ def test_full_size_properties(bank64):
     h, t, f = O.decode_location(gl)
     for s in sig:
         assert (np.abs(f - s["r0"]) < 1000).any(), s
+
+
+@pytest.mark.parametrize("part,name", [(FDAS.NegativeAccelerations, "neg"), (FDAS.PositiveAccelerations, "pos")])
+@pytest.mark.parametrize("thr_key", ["", "_chi2"])
+def test_fpga_ring_list(part, name, thr_key):
+    """The reference detectors' 64-slot ring, from an injected FOP (FP32, bit-exact)."""
+    g = load_golden("n4096")
+    thr = g["thresholds" + thr_key]
+    p = make_pipeline(4096, log=io.StringIO())
+    assert p.inject_FOP(g["fop_ref"], FDAS.A)
+    assert p.perform_harmonic_summing(thr, part, FDAS.A)
+    loc = np.zeros(4096, dtype=np.uint32)
+    pwr = np.zeros(4096, dtype=np.float32)
+    assert p.retrieve_candidates_ring(loc, pwr, part, FDAS.A)
+    el, ep = O.ring_list(g["det_loc_ref" + thr_key], g["det_pwr_ref" + thr_key], name)
+    assert np.array_equal(loc, el) and np.array_equal(pwr, ep)
+    # every ring entry is a reference candidate (main_gtest.cpp:192-228)
+    if (loc != O.INVALID_LOCATION).any():
+        validate_harmonic_summing(loc, pwr, g["det_loc_ref" + thr_key], g["det_pwr_ref" + thr_key])
+    assert not p.retrieve_candidates_ring(loc, pwr, FDAS.AllAccelerations, FDAS.A)

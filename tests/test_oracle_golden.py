@@ -117,3 +117,18 @@ def test_compat_list_rule():
     assert np.all(np.diff(kept.astype(np.int64)) > 0)
     assert P[:512].min() >= np.sort(pwr)[-512]
     assert np.all(L[512:] == O.INVALID_LOCATION) and np.all(P[512:] == -1.0)
+
+
+def test_ring_list_matches_fpga_scan_order():
+    """ring_list keeps the last 64 (group, bundle) events of the scan, slot = index mod 64."""
+    # 70 events on plane 1 in the negative half: template 0, bins 0, 2, 4, ... (one hit per bundle)
+    f = np.arange(70) * 2
+    loc = O.encode_location(np.ones(70, dtype=np.int64), np.zeros(70, dtype=np.int64), f)
+    pwr = np.arange(70, dtype=np.float32)
+    L, P = O.ring_list(loc, pwr, "neg")
+    L = L.reshape(8, 64, 8)
+    # events 6..69 survive; event e sits in slot e % 64, lane 0
+    h, t, fb = O.decode_location(L[0, :, 0])
+    assert sorted(fb.tolist()) == sorted((np.arange(6, 70) * 2).tolist())
+    assert L[0, 6 % 64, 0] == loc[6] and L[0, 69 % 64, 0] == loc[69]
+    assert np.all(L[1:] == O.INVALID_LOCATION)
