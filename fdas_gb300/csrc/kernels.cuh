@@ -12,7 +12,6 @@ constexpr int kMaxPlanes = 16;       // harmonic planes supported by the kernels
 constexpr int kHsBins = 256;         // bins per harmonic-summing work item
 constexpr int kSortCap = 8192;       // boundary records one CTA ranks in shared memory
 constexpr int kMaxCompat = 2048;     // entries per plane of the fixed-size list
-constexpr int kEmitBuf = 1024;       // candidate records staged per harmonic-summing CTA
 constexpr int kSelBuckets = 2048;    // power buckets of the top-K selection (float bits 30..20)
 
 // device status bits (per buffer set)

@@ -68,18 +68,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, long long timeo
   }
 }
 
-// Candidate staging: each warp collects its records in a shared-memory
-// buffer (warp ballot -> one slot range per batch) and moves a full buffer to
-// the global list with a single atomic reservation.
-constexpr int kWarpBuf = 32;
-constexpr int kHsMaxWarps = 16;  // templates per half <= 64
-
-struct EmitBuf {
-  unsigned pc[kMaxPlanes];                 // hits per plane of this CTA
-  unsigned long long key[kHsMaxWarps][kWarpBuf];
-  float pwr[kHsMaxWarps][kWarpBuf];
-};
-
+// one record appended to the global list (single-thread use)
 __device__ __forceinline__ void global_append(unsigned long long *keys, float *pwrs, unsigned *total, int cap,
                                               int *status, unsigned long long key, float pwr) {
   const unsigned g = atomicAdd(total, 1u);
@@ -91,51 +80,11 @@ __device__ __forceinline__ void global_append(unsigned long long *keys, float *p
   }
 }
 
-// warp-synchronous: move this warp's staged records to the global list
-__device__ __forceinline__ void warp_flush(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p) {
-  __syncwarp();
-  const int lane = threadIdx.x & 31;
-  unsigned base = 0;
-  if (lane == 0 && wcount) base = atomicAdd(p.cand_total, wcount);
-  base = __shfl_sync(0xffffffffu, base, 0);
-  for (unsigned i = lane; i < wcount; i += 32) {
-    const unsigned g = base + i;
-    if (g < (unsigned)p.cand_cap) {
-      p.cand_key[g] = eb.key[warp][i];
-      p.cand_pwr[g] = eb.pwr[warp][i];
-    }
-  }
-  if (lane == 0 && wcount && base + wcount > (unsigned)p.cand_cap) atomicOr(p.status, kStatusCandidateOverflow);
-  __syncwarp();
-  wcount = 0;
-}
-
-// warp-synchronous emission of the lanes in `hm` (all lanes call this)
-__device__ __forceinline__ void warp_emit(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
-                                          unsigned hm, int plane, int row, int bin, float pwr) {
-  const int lane = threadIdx.x & 31;
-  const unsigned n = __popc(hm);
-  if (wcount + n > (unsigned)kWarpBuf) warp_flush(eb, warp, wcount, p);
-  if ((hm >> lane) & 1u) {
-    const unsigned slot = wcount + __popc(hm & ((1u << lane) - 1u));
-    eb.key[warp][slot] = cand_key(plane, row, bin);
-    eb.pwr[warp][slot] = pwr;
-  }
-  if (lane == 0) atomicAdd(&eb.pc[plane], n);
-  wcount += n;
-}
-
-__device__ __forceinline__ void warp_recheck(const HsumParams &p, unsigned nm, int plane, int row, int bin) {
-  const int lane = threadIdx.x & 31;
-  unsigned base = 0;
-  if (lane == 0) base = atomicAdd(p.rc_count, (unsigned)__popc(nm));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if ((nm >> lane) & 1u) {
-    const unsigned idx = base + __popc(nm & ((1u << lane) - 1u));
-    if (idx < (unsigned)p.rc_cap) p.rc_list[idx] = make_uint4((unsigned)plane, (unsigned)row, (unsigned)bin, 0u);
-    else atomicOr(p.status, kStatusRecheckOverflow);
-  }
-}
+// Per-CTA hit counts per plane (shared memory), added to the global counts
+// when the CTA ends.
+struct EmitBuf {
+  unsigned pc[kMaxPlanes];  // hits per plane of this CTA
+};
 
 // Persistent harmonic summing.  Work item = (256-bin block, sign half),
 // handed out dynamically through a global counter.  A CTA has NW consumer
@@ -223,43 +172,76 @@ __device__ __forceinline__ void add_rows(float (&acc)[4][8], const float (&c0)[8
     for (int e = 0; e < 8; ++e) acc[k][e] += k < KS ? c0[e] : c1[e];
 }
 
-// plane j >= 2 added to the tile, generic form (any j, runtime)
-__device__ __forceinline__ void add_plane_generic(float (&acc)[4][8], const float *stage, const HsumParams &p, int j,
-                                                  int f0, int t0, int F, int sgn) {
-  const int a0 = (f0 / j) & ~3;
-  const int bw = p.bw[j], bh = p.bh[j];
-  const int rb = t0 / j;
-  const int kstar = j - (t0 - rb * j);
-  const float *r0 = stage + p.soff[j] + srow(rb, bh, sgn) * bw - a0;
-  const float *r1 = r0 + sgn * bw;
-  float c0[8], c1[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    const int o = (F + e) / j;
-    c0[e] = r0[o];
-    c1[e] = r1[o];
-  }
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-#pragma unroll
-    for (int e = 0; e < 8; ++e) acc[k][e] += k < kstar ? c0[e] : c1[e];
-}
+// Emission of plane `plane` (0-based) from the tile values; called by the
+// whole warp when some lane's tile reached the lower edge of the plane's band.
+// Out of line, with the tile passed by value, so the hot loop keeps its
+// accumulators in registers and stays small.  Each lane builds its hit mask,
+// a warp prefix sum gives every lane its slots in the warp's record buffer.
+struct Tile32 {
+  float v[32];  // v[8 k + e]: template |t| = t0 + k, bin F + e
+};
 
-// Emission of plane `plane` (0-based) from the accumulators; whole warp.
-__device__ __forceinline__ void emit_plane(EmitBuf &eb, int warp, unsigned &wcount, const HsumParams &p,
-                                           const float (&acc)[4][8], int plane, int H, int sgn, int t0, int F) {
+__device__ __noinline__ void emit_tile(EmitBuf &eb, const HsumParams &p, Tile32 tile,
+                                       int plane, int H, int sgn, int t0, int F) {
+  const int lane = threadIdx.x & 31;
   const float hi = p.hi[plane], lo = p.lo[plane];
+  unsigned hmask = 0, nmask = 0;
 #pragma unroll
-  for (int kk = 0; kk < 4; ++kk) {
+  for (int c = 0; c < 32; ++c) {
+    const float a = tile.v[c];  // -inf for masked cells
+    if (a > hi) hmask |= 1u << c;
+    else if (a >= lo) nmask |= 1u << c;
+  }
+  // near-threshold cells go to the FP64 recheck list
+  unsigned nn = __popc(nmask);
+  unsigned ntot = nn;
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const float a = acc[kk][e];  // -inf for masked cells
-      const bool hit = a > hi;
-      const bool near = !hit && a >= lo;
-      const unsigned hm = __ballot_sync(0xffffffffu, hit);
-      if (hm) warp_emit(eb, warp, wcount, p, hm, plane, H + sgn * (t0 + kk), F + e, a);
-      const unsigned nm = __ballot_sync(0xffffffffu, near);
-      if (nm) warp_recheck(p, nm, plane, H + sgn * (t0 + kk), F + e);
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned u = __shfl_up_sync(0xffffffffu, ntot, o);
+    if (lane >= o) ntot += u;
+  }
+  const unsigned nall = __shfl_sync(0xffffffffu, ntot, 31);
+  if (nall) {
+    unsigned base = 0;
+    if (lane == 31) base = atomicAdd(p.rc_count, nall);
+    base = __shfl_sync(0xffffffffu, base, 31) + ntot - nn;
+    while (nmask) {
+      const int c = __ffs(nmask) - 1;
+      nmask &= nmask - 1;
+      if (base < (unsigned)p.rc_cap)
+        p.rc_list[base] = make_uint4((unsigned)plane, (unsigned)(H + sgn * (t0 + (c >> 3))), (unsigned)(F + (c & 7)), 0u);
+      else
+        atomicOr(p.status, kStatusRecheckOverflow);
+      ++base;
+    }
+  }
+  // hits: one warp-aggregated reservation in the global list, then every lane
+  // stores its own records there directly (no staging, no further atomics)
+  const unsigned hn = __popc(hmask);
+  unsigned incl = hn;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total) {
+    unsigned base = 0;
+    if (lane == 31) base = atomicAdd(p.cand_total, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    unsigned g = base + incl - hn;
+    while (hmask) {
+      const int c = __ffs(hmask) - 1;
+      hmask &= hmask - 1;
+      if (g < (unsigned)p.cand_cap) {
+        p.cand_key[g] = cand_key(plane, H + sgn * (t0 + (c >> 3)), F + (c & 7));
+        p.cand_pwr[g] = tile.v[c];
+      }
+      ++g;
+    }
+    if (lane == 0) {
+      atomicAdd(&eb.pc[plane], total);
+      if (base + total > (unsigned)p.cand_cap) atomicOr(p.status, kStatusCandidateOverflow);
     }
   }
 }
@@ -331,7 +313,6 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
   } else {
     // ------------------------------------------------------------ consumers
     const int t0 = 4 * warp;
-    unsigned wcount = 0;
     for (int s = 0;; ++s) {
       const int st = s % kHsStages, use = s / kHsStages;
       if (!mbar_wait_parity(full + st, use & 1, p.timeout_ns)) {
@@ -373,8 +354,16 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
         }
       };
       load_plane1();
-      // bit j-1: some lane of the warp reached the band of plane j (warp-uniform)
-      unsigned trig = __any_sync(0xffffffffu, max32(acc) >= p.trig[0]) ? 1u : 0u;
+      auto emit = [&](int plane) {
+        Tile32 tile;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int e = 0; e < 8; ++e) tile.v[8 * kk + e] = acc[kk][e];
+        emit_tile(eb, p, tile, plane, H, sgn, t0, F);
+      };
+      // rare: some lane of the warp reached the band of the plane (warp-uniform)
+      if (__any_sync(0xffffffffu, max32(acc) >= p.trig[0])) emit(0);
       hs_sfor<MAXP - 1>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value + 2;
         if (j <= P) {
@@ -422,27 +411,14 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
               default: add_rows<4>(acc, c0, c1); break;
             }
           }
-          if (__any_sync(0xffffffffu, max32(acc) >= p.trig[j - 1])) trig |= 1u << (j - 1);
+          if (__any_sync(0xffffffffu, max32(acc) >= p.trig[j - 1])) emit(j - 1);
         }
       });
-
-      // ---- rare: recompute the sums plane by plane (same values, same order)
-      // and emit the planes whose band was reached
-      if (trig) {
-        load_plane1();
-        const int last = 32 - __clz(trig);  // highest plane needed
-#pragma unroll 1
-        for (int j = 1; j <= last; ++j) {
-          if (j > 1) add_plane_generic(acc, stage, p, j, f0, t0, F, sgn);
-          if ((trig >> (j - 1)) & 1u) emit_plane(eb, warp, wcount, p, acc, j - 1, H, sgn, t0, F);
-        }
-      }
 
       // release the stage to the producer
       __syncwarp();
       if (lane == 0) mbar_arrive(empty + st);
     }
-    warp_flush(eb, warp, wcount, p);
   }
 
   // ---- per-plane hit counts of the CTA
