@@ -85,8 +85,52 @@ __device__ __forceinline__ void sfor(F &&f) {
 }
 
 // ------------------------------------------------------------ complex ops
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add / subtract as one packed FP32 pair instruction (add.rn.f32x2 /
+// sub.rn.f32x2, sm_100 and later): each half is an ordinary round-to-nearest
+// FP32 add, so results equal two scalar adds.
+__device__ __forceinline__ unsigned long long f2_pack(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
+// a + c b and a - c b for a real constant c, as packed fused multiply-adds
+__device__ __forceinline__ float2 cfma_real(float c, float2 b, float2 a) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2_pack(make_float2(c, c))), "l"(f2_pack(b)), "l"(f2_pack(a)));
+  return f2_unpack(r);
+}
+// c b for a real c, as one packed multiply
+__device__ __forceinline__ float2 cscale(float c, float2 b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(make_float2(c, c))), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
+// t + S i d and t - S i d (rotation by +-90 degrees folded into scalar adds)
+template <int S>
+__device__ __forceinline__ void add_sub_i(float2 t, float2 d, float2 &plus, float2 &minus) {
+  if constexpr (S > 0) {
+    plus = make_float2(t.x - d.y, t.y + d.x);
+    minus = make_float2(t.x + d.y, t.y - d.x);
+  } else {
+    plus = make_float2(t.x + d.y, t.y - d.x);
+    minus = make_float2(t.x - d.y, t.y + d.x);
+  }
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
@@ -135,12 +179,10 @@ __device__ __forceinline__ void dft2(float2 *v) {
 template <int S, int OFF, int STRIDE>
 __device__ __forceinline__ void dft4(float2 *v) {
   float2 x0 = v[OFF], x1 = v[OFF + STRIDE], x2 = v[OFF + 2 * STRIDE], x3 = v[OFF + 3 * STRIDE];
-  float2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3);
-  float2 t3 = rot<S, 4, 1>(csub(x1, x3));
+  float2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), d = csub(x1, x3);
   v[OFF] = cadd(t0, t2);
   v[OFF + 2 * STRIDE] = csub(t0, t2);
-  v[OFF + STRIDE] = cadd(t1, t3);
-  v[OFF + 3 * STRIDE] = csub(t1, t3);
+  add_sub_i<S>(t1, d, v[OFF + STRIDE], v[OFF + 3 * STRIDE]);
 }
 
 template <int S, int OFF, int STRIDE>
@@ -150,15 +192,18 @@ __device__ __forceinline__ void dft8(float2 *v) {
   float2 o[4] = {v[OFF + STRIDE], v[OFF + 3 * STRIDE], v[OFF + 5 * STRIDE], v[OFF + 7 * STRIDE]};
   dft4<S, 0, 1>(e);
   dft4<S, 0, 1>(o);
-  float2 o1 = rot<S, 8, 1>(o[1]), o2 = rot<S, 8, 2>(o[2]), o3 = rot<S, 8, 3>(o[3]);
+  // o1 w^1 = r (1 + S i) o1 = r u1, o3 w^3 = r (-1 + S i) o3 = r u3, o2 w^2 = S i o2
+  const float2 u1 = S > 0 ? make_float2(o[1].x - o[1].y, o[1].y + o[1].x)
+                          : make_float2(o[1].x + o[1].y, o[1].y - o[1].x);
+  const float2 u3 = S > 0 ? make_float2(-(o[3].x + o[3].y), o[3].x - o[3].y)
+                          : make_float2(o[3].y - o[3].x, -(o[3].x + o[3].y));
   v[OFF] = cadd(e[0], o[0]);
   v[OFF + 4 * STRIDE] = csub(e[0], o[0]);
-  v[OFF + STRIDE] = cadd(e[1], o1);
-  v[OFF + 5 * STRIDE] = csub(e[1], o1);
-  v[OFF + 2 * STRIDE] = cadd(e[2], o2);
-  v[OFF + 6 * STRIDE] = csub(e[2], o2);
-  v[OFF + 3 * STRIDE] = cadd(e[3], o3);
-  v[OFF + 7 * STRIDE] = csub(e[3], o3);
+  v[OFF + STRIDE] = cfma_real(kRsqrt2, u1, e[1]);
+  v[OFF + 5 * STRIDE] = cfma_real(-kRsqrt2, u1, e[1]);
+  add_sub_i<S>(e[2], o[2], v[OFF + 2 * STRIDE], v[OFF + 6 * STRIDE]);
+  v[OFF + 3 * STRIDE] = cfma_real(kRsqrt2, u3, e[3]);
+  v[OFF + 7 * STRIDE] = cfma_real(-kRsqrt2, u3, e[3]);
 }
 
 template <int S, int R, int OFF, int STRIDE>
@@ -413,7 +458,7 @@ __device__ __forceinline__ void ifft2_pass2(const float2 *buf, int h, int lane, 
     constexpr int q = decltype(Q)::value;
     sfor<4>([&](auto P2) {
       constexpr int p2 = 2 * decltype(P2)::value + 1;
-      u[8 * q + p2] = make_float2(sg * u[8 * q + p2].x, sg * u[8 * q + p2].y);
+      u[8 * q + p2] = cscale(sg, u[8 * q + p2]);
     });
     dft8<+1, 8 * q, 1>(u);
     // twiddle e^(2 pi i d1 p1 / 64); constants differ per lane group
