@@ -89,6 +89,7 @@ SIGNATURES = {
     "fdas_get_stream": (_P, [_P, _INT]),
     "fdas_get_counters": (_INT, [_P, _INT, _P, _U32]),
     "fdas_retrieve_candidates_ring": (_INT, [_P, _P, _P, _INT, _INT]),
+    "fdas_ft_convolution_noalloc": (_INT, [_P, _U32, _P, _INT, _U32, _U32, _INT, _P, ctypes.c_uint64, _P, _P]),
     "fdas_version": (ctypes.c_char_p, []),
 }
 

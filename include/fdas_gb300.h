@@ -252,6 +252,54 @@ void *fdas_get_stream(fdas_handle *h, fdas_buffer_set ab);
  * p, [19 + p] hits of plane p certain to enter its fixed-size list (p < 16). */
 fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out, uint32_t n);
 
+/* ------------------------------------------------------------------------
+ * FT convolution that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory when they search: a pipeline
+ * whose device memory all belongs to its own pool allocator with a fixed
+ * budget, a real-time search that must not hit an out-of-memory error in the
+ * middle of an observation, or code where cudaMalloc / cudaFree would
+ * synchronise the device and stall the caller's other streams.  It does the
+ * work of fdas_perform_input_tiling + fdas_perform_ft_convolution (same
+ * kernels, same FOP values) on a spectrum and into a FOP that the caller holds
+ * in device memory.  The tile spectra, the scaled template spectra and the
+ * twiddle table live in a static device scratch array of the library (about
+ * 8 MB, present while the library is loaded); no device or host memory is
+ * allocated, by this call or by anything it calls.
+ *
+ *  d_spectrum  n_bins complex bins, device memory, 8-byte aligned
+ *  d_templates n_templates x 2048 template spectra, device memory, in the
+ *              p4 order of fdas_templates_85_350_ft_p4.npy (FFT_P4) or in
+ *              natural order (FFT_NATURAL); TIME_DOMAIN is UNSUPPORTED here
+ *  tile_overlap overlap-save overlap O (420 for the 421-tap bank); tiles of
+ *              2048 bins advance by 2048 - O
+ *  which       FOP rows computed (the other part's rows are left untouched)
+ *  d_fop       n_templates x fop_stride floats, device memory, row = template
+ *              + n_templates / 2; fop_stride >= n_bins
+ *  d_status    NULL, or a device int32 that the caller has set to zero: a
+ *              kernel wait that timed out (2 s) ORs 16 into it and leaves the
+ *              FOP incomplete
+ *  stream      cudaStream_t (NULL: the default stream); the call only enqueues
+ *
+ * Limits: ceil(n_bins / (2048 - O)) <= FDAS_NOALLOC_MAX_TILES (2^19 bins and
+ * more at O = 420) and n_templates <= FDAS_NOALLOC_MAX_TEMPLATES; larger sizes
+ * return FDAS_ERR_CAPACITY before any work is enqueued.  Failures are reported
+ * by the status only (no message is stored: storing one would allocate).
+ *
+ * The first call on a device, with that device current, looks up the scratch
+ * address (cudaGetSymbolAddress) and copies the twiddle table into it with a
+ * synchronous copy; make that first call before capturing a stream.  All calls
+ * on one device share the one scratch area: two calls whose work overlaps on
+ * the device (different streams with no ordering between them, or several
+ * host threads) race and corrupt each other's FOP.  Order them on one stream.
+ * ---------------------------------------------------------------------- */
+#define FDAS_NOALLOC_MAX_TILES 384u
+#define FDAS_NOALLOC_MAX_TEMPLATES 128u
+fdas_status fdas_ft_convolution_noalloc(const fdas_complex *d_spectrum, uint32_t n_bins,
+                                        const fdas_complex *d_templates, fdas_template_layout layout,
+                                        uint32_t n_templates, uint32_t tile_overlap, fdas_fop_part which,
+                                        float *d_fop, uint64_t fop_stride, int32_t *d_status, void *stream);
+
 /* Library version string. */
 const char *fdas_version(void);
 
