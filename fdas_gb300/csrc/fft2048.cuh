@@ -68,7 +68,8 @@ constexpr double cexpr_cos_frac(long j, long n) {
     default: return taylor_cos(b);
   }
 }
-constexpr double cexpr_sin_frac(long j, long n) { return cexpr_cos_frac(j - n / 4, n) ; }
+// sin(2 pi j / n) = cos(2 pi (4 j - n) / 4 n), exact for every n
+constexpr double cexpr_sin_frac(long j, long n) { return cexpr_cos_frac(4 * j - n, 4 * n); }
 
 template <int N, int J> constexpr float kCos = (float)cexpr_cos_frac(J, N);
 template <int N, int J> constexpr float kSin = (float)cexpr_sin_frac(J, N);
@@ -397,22 +398,19 @@ namespace fdas {
 constexpr int kEx2Pitch = 33;                 // complex values per row of the pair buffer
 constexpr int kEx2Floats = 64 * kEx2Pitch * 2;  // floats per warp pair (>= 2048 complex)
 
-struct Twiddle2 {
-  float2 lo[4];  // w^(p k1), k1 < 4
-  float2 hi[8];  // w^(4 p k2), k2 < 8
-};
+// Twiddles w^(m p) of the two-warp transform, m < 32, p < 64, stored at
+// [64 m + p] (16 KB of shared memory per CTA, shared by its warp pairs).
+constexpr int kTw2Floats = 2 * 32 * 64;
 
-__device__ __forceinline__ Twiddle2 load_twiddle2(const float2 *__restrict__ table, int p) {
-  Twiddle2 t;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) t.lo[k] = __ldg(table + ((k * p) & 2047));
-#pragma unroll
-  for (int k = 0; k < 8; ++k) t.hi[k] = __ldg(table + ((4 * k * p) & 2047));
-  return t;
+__device__ __forceinline__ void fill_twiddle2(float2 *twt, const float2 *__restrict__ table) {
+  for (int i = threadIdx.x; i < 32 * 64; i += blockDim.x) {
+    const int m = i >> 6, p = i & 63;
+    twt[i] = __ldg(table + ((m * p) & 2047));
+  }
 }
 
 // Pass 1 + twiddle + write to the pair buffer.  v[a] holds Y[64 a + p] on entry.
-__device__ __forceinline__ void ifft2_pass1(float2 *v, const Twiddle2 &tw, float2 *buf, int p) {
+__device__ __forceinline__ void ifft2_pass1(float2 *v, const float2 *twt, float2 *buf, int p) {
   dft32<+1, 0>(v);
   // V_p[m] = Z_p[m] w^(m p), m = k1 + 4 k2 sits in v[8 k1 + k2]
   sfor<4>([&](auto K1) {
@@ -420,14 +418,8 @@ __device__ __forceinline__ void ifft2_pass1(float2 *v, const Twiddle2 &tw, float
     sfor<8>([&](auto K2) {
       constexpr int k2 = decltype(K2)::value;
       constexpr int idx = 8 * k1 + k2;
-      if constexpr (k1 == 0 && k2 == 0) {
-      } else if constexpr (k1 == 0) {
-        v[idx] = cmul(v[idx], tw.hi[k2]);
-      } else if constexpr (k2 == 0) {
-        v[idx] = cmul(v[idx], tw.lo[k1]);
-      } else {
-        v[idx] = cmul(v[idx], cmul(tw.lo[k1], tw.hi[k2]));
-      }
+      constexpr int m = k1 + 4 * k2;
+      if constexpr (m != 0) v[idx] = cmul(v[idx], twt[64 * m + p]);
     });
   });
   float2 *row = buf + kEx2Pitch * p;

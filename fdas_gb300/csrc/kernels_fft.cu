@@ -184,6 +184,7 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
   const int pair = warp >> 1, h = warp & 1;
   const int tp = 32 * h + lane;  // thread of the pair
   float *buf_f = reinterpret_cast<float *>(smem_f4) + pair * kEx2Floats;
+  float2 *twt = reinterpret_cast<float2 *>(reinterpret_cast<float *>(smem_f4) + kPairsPerCta * kEx2Floats);
   float2 *buf = reinterpret_cast<float2 *>(buf_f);
   uint64_t *bar = &bars[pair];
   const int n_items = p.n_tiles * p.n_rows;
@@ -193,8 +194,8 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
     mbar_init(bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  pair_sync(pair);
-  const Twiddle2 tw = load_twiddle2(p.twiddle, tp);
+  fill_twiddle2(twt, p.twiddle);
+  __syncthreads();
   if (item < n_items && tp == 0)
     prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + item % p.n_rows) * kTile, bar);
   uint32_t parity = 0;
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
       v[a] = cmul(v[a], buf[64 * a + tp]);
     });
     pair_sync(pair);  // template read by both warps: the buffer takes the exchange
-    ifft2_pass1(v, tw, buf, tp);
+    ifft2_pass1(v, twt, buf, tp);
     pair_sync(pair);  // exchange written
     const int next = item + stride;
     float pw[32];
@@ -323,7 +324,7 @@ cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
     const long long ctas = (items + kWarpsPerCta - 1) / kWarpsPerCta;
     ftc_kernel<<<(int)(ctas < n_sm ? ctas : n_sm), 256, smem, s>>>(p);
   } else {
-    const int smem = kPairsPerCta * kEx2Floats * (int)sizeof(float);
+    const int smem = (kPairsPerCta * kEx2Floats + kTw2Floats) * (int)sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(ftc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     const long long ctas = (items + kPairsPerCta - 1) / kPairsPerCta;
