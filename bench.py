@@ -372,6 +372,192 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ served form
+def served_spectrum(n, seed):
+    """Seeded unit-power Gaussian trial of 2n samples with 0-2 accelerated
+    signals (random z in [-42, 42], 1-8 harmonics)."""
+    from fdas_gb300 import synth
+    rng = np.random.default_rng(seed)
+    amp = 0.05 * np.sqrt((1 << 15) / n)
+    sig = [dict(r0=float(rng.uniform(0.05, 0.45) * n), z=float(rng.uniform(-42, 42)),
+                n_harm=int(rng.integers(1, 9)), amp=amp) for _ in range(int(rng.integers(0, 3)))]
+    return synth.spectrum(synth.timeseries(2 * n, sig, seed=seed), n)[0]
+
+
+def run_served(args):
+    """Open request loop: Poisson arrivals at --rate searches/s; each request is
+    a trial of 2^16..2^22 samples (2^15..2^21 bins), the 85-template bank or
+    its z = -21..+21 half, 4, 8 or 16 planes, chi-square FAR 1e-6 thresholds.
+    The request server (continuous batching, slots admitted by FOP bytes
+    against free HBM) against the plain path per request (one search at a time
+    through fdas_launch / fdas_wait, first come first served)."""
+    import torch
+    from scipy.stats import gamma
+    from fdas_gb300.fdas import FDAS
+    from fdas_gb300.server import Server, HALF_BANK
+    from fdas_gb300.templates import template_bank
+    torch.cuda.set_device(0)
+    bank = template_bank()
+    rng = np.random.default_rng(2025)
+    sizes = [1 << k for k in range(15, 22)]
+    pool = {n: [served_spectrum(n, 100 * k + i) for i in range(2)] for k, n in enumerate(sizes)}
+    thr = {P: np.array([gamma.isf(1e-6, k) for k in range(1, P + 1)], dtype=np.float32) for P in (4, 8, 16)}
+    n_req = args.requests
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
+    reqs = [(sizes[int(rng.integers(0, len(sizes)))], bool(rng.integers(0, 2)), int(rng.choice([4, 8, 16])),
+             int(rng.integers(0, 2))) for _ in range(n_req)]
+
+    def rows_of(half):
+        return HALF_BANK if half else (0, 85)
+
+    def stats(lat, wall):
+        lat = np.asarray(lat)
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "searches_per_s": n_req / wall}
+
+    # ---- served
+    with Server(bank, max_bins=1 << 21, max_slots=args.slots) as srv:
+        for n in sizes:  # warm-up: one request per length class creates the slots
+            for half in (False, True):
+                srv.result(srv.submit(pool[n][0], thr[8], rows_of(half)))
+        ids, t_sub = [], []
+        t0 = time.perf_counter()
+        for (n, half, P, k), ta in zip(reqs, arrivals):
+            dt = t0 + ta - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            t_sub.append(time.perf_counter())
+            ids.append(srv.submit(pool[n][k], thr[P], rows_of(half)))
+        lat = [srv.result(rid)[3] for rid in ids]
+        # each request's result time = its submit time + the server-measured latency
+        wall = max(ts + l * 1e-3 for ts, l in zip(t_sub, lat)) - t0
+        served = stats(lat, wall)
+        served["peak_in_flight"] = srv.stats()["peak_in_flight"]
+
+    # ---- plain path per request: one handle per length class, searches one at a time
+    log = open(os.devnull, "w")
+    handles = {}
+    for n in sizes:
+        h = FDAS(log)
+        assert h.initialise_accelerator(n, n_planes=16), h.last_error
+        assert h.upload_templates(bank, FDAS.A), h.last_error
+        handles[n] = h
+    loc = np.zeros(16 * 512, np.uint32)
+    pwr = np.zeros(16 * 512, np.float32)
+
+    def plain_one(n, half, P, k):
+        h = handles[n]
+        r0, nt = rows_of(half)
+        assert h.reshape(n, r0, nt, 0, P), h.last_error
+        assert h.launch(pool[n][k], thr[P], loc, pwr, FDAS.AllAccelerations, FDAS.A), h.last_error
+        assert h.wait(FDAS.A), h.last_error
+        h.retrieve_candidate_list(FDAS.A)
+
+    for n in sizes:
+        plain_one(n, False, 8, 0)
+    lat = []
+    t0 = time.perf_counter()
+    for (n, half, P, k), ta in zip(reqs, arrivals):
+        dt = t0 + ta - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        plain_one(n, half, P, k)
+        lat.append((time.perf_counter() - (t0 + ta)) * 1e3)
+    plain = stats(lat, time.perf_counter() - t0)
+    line = {"form": "served", "metric": "served searches: p50/p99 latency (submit to candidate list) and searches/s",
+            "unit": "ms", "rate_per_s": args.rate, "requests": n_req, "slots": args.slots,
+            "mix": "2^15..2^21 bins (uniform in log2), full 85 or half 43 template bank, 4/8/16 planes, "
+                   "0-2 signals, chi-square FAR 1e-6", "served": served, "plain_per_request": plain,
+            "data": "synthetic"}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ batched form
+def run_batched(args):
+    """256 dedispersed trials of uneven length (log-uniform 2^18..2^22 samples,
+    i.e. 2^17..2^21 bins), 0-2 accelerated signals each (z in [-42, 42], 1-8
+    harmonics), 85-template bank, 8 planes, chi-square FAR 1e-6: one batched
+    pass (one FT-convolution launch over all trials' items, CUDA graph,
+    autotuned) against the plain path searching the same trials one by one."""
+    import torch
+    from scipy.stats import gamma
+    from fdas_gb300.batch import Batch
+    from fdas_gb300.fdas import FDAS
+    from fdas_gb300.templates import template_bank
+    torch.cuda.set_device(0)
+    bank = template_bank()
+    rng = np.random.default_rng(4242)
+    n_tr = args.trials
+    n_samp = np.exp(rng.uniform(np.log(2 ** 18), np.log(2 ** 22), n_tr)).astype(np.int64) // 2 * 2
+    n_bins = (n_samp // 2).astype(np.uint32)
+    thr = np.array([gamma.isf(1e-6, k) for k in range(1, 9)], dtype=np.float32)
+    # synthetic spectra made on the GPU (input preparation, not timed)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    specs = []
+    for i in range(n_tr):
+        ns = int(n_samp[i])
+        x = torch.randn(ns, device="cuda", generator=g, dtype=torch.float64)
+        u = torch.arange(ns, device="cuda", dtype=torch.float64) / ns
+        for _ in range(int(rng.integers(0, 3))):
+            r0, z, nh = rng.uniform(0.05, 0.45) * ns / 2, rng.uniform(-42, 42), int(rng.integers(1, 9))
+            amp = 0.05 * np.sqrt((1 << 15) / (ns / 2))
+            ph = 2 * np.pi * (r0 * u + 0.5 * z * u * u)
+            for h in range(1, nh + 1):
+                x += amp * torch.cos(h * ph)
+        X = torch.fft.rfft(x.float().double())[: ns // 2] / np.sqrt(ns)
+        specs.append(torch.view_as_real(X.to(torch.complex64)).contiguous())
+    d_all = torch.cat([s.reshape(-1) for s in specs])
+    torch.cuda.synchronize()
+    total_bins = int(n_bins.sum())
+
+    # ---- batched
+    b = Batch(bank, n_bins, autotune=not args.no_autotune)
+    b.set_inputs_device(d_all.data_ptr())
+    t = time.perf_counter()
+    b.run(thr)  # autotune + capture + first replay
+    t_setup = time.perf_counter() - t
+    for _ in range(args.warmup):
+        b.run(thr)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        b.run(thr)
+        times.append(time.perf_counter() - t)
+    batched_s = float(np.median(times))
+    info = b.info()
+    n_cand = sum(b.trial(i).retrieve_candidate_list(FDAS.A, capacity=0)[1] for i in range(n_tr))
+    b.close()
+
+    # ---- plain path: the same trials one at a time on one handle (reshaped per trial)
+    log = open(os.devnull, "w")
+    h = FDAS(log)
+    assert h.initialise_accelerator(int(n_bins.max())), h.last_error
+    assert h.upload_templates(bank, FDAS.A), h.last_error
+    offs = np.concatenate([[0], np.cumsum(n_bins.astype(np.int64))])
+
+    def plain_pass():
+        for i in range(n_tr):
+            assert h.reshape(int(n_bins[i])), h.last_error
+            assert h.enqueue_search_device(d_all.data_ptr() + 8 * int(offs[i]), thr, FDAS.AllAccelerations,
+                                           FDAS.A), h.last_error
+        assert h.synchronize(FDAS.A)
+
+    plain_pass()
+    pt = []
+    for _ in range(max(1, args.steps // 2)):
+        t = time.perf_counter()
+        plain_pass()
+        pt.append(time.perf_counter() - t)
+    plain_s = float(np.median(pt))
+    line = {"form": "batched", "metric": "batched searches/s (trials of uneven length)", "unit": "searches/s",
+            "value": n_tr / batched_s, "ms_per_batch": batched_s * 1e3, "trials": n_tr, "total_bins": total_bins,
+            "fop_gb": 4 * 85 * total_bins / 1e9, "plain_value": n_tr / plain_s, "plain_ms_per_batch": plain_s * 1e3,
+            "speedup_vs_plain": plain_s / batched_s, "autotune": info, "setup_s": t_setup,
+            "candidates": int(n_cand), "steps": args.steps, "warmup": args.warmup,
+            "timing": "host clock around graph replays (each ~100 ms), median", "data": "synthetic (seeded, on GPU)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -385,9 +571,22 @@ def main():
                     help="Gaussian noise without the injected signals (profiling the no-candidate path)")
     ap.add_argument("--bins", type=int, default=N_BINS,
                     help="spectrum bins; the reported workload is 2^21, smaller values are for ncu captures")
+    ap.add_argument("--trials", type=int, default=256, help="batched form: number of trials")
+    ap.add_argument("--no-autotune", action="store_true", help="batched form: default tuning")
+    ap.add_argument("--form", default="plain", choices=["plain", "served", "batched"],
+                    help="served: the request server under Poisson arrivals (prints its own JSON line)")
+    ap.add_argument("--rate", type=float, default=200.0, help="served form: arrival rate (searches/s)")
+    ap.add_argument("--requests", type=int, default=400, help="served form: number of requests")
+    ap.add_argument("--slots", type=int, default=8, help="served form: searches in flight at most")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.form == "served":
+        run_served(args)
+        return
+    if args.form == "batched":
+        run_batched(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -89,6 +89,26 @@ SIGNATURES = {
     "fdas_get_stream": (_P, [_P, _INT]),
     "fdas_get_counters": (_INT, [_P, _INT, _P, _U32]),
     "fdas_retrieve_candidates_ring": (_INT, [_P, _P, _P, _INT, _INT]),
+    "fdas_server_default_config": (None, [_P]),
+    "fdas_server_create": (_INT, [_P, _P, _INT, _U32, _U32, _P]),
+    "fdas_server_submit": (_INT, [_P, _P, _U32, _U32, _U32, _U32, _P, _P]),
+    "fdas_server_wait": (_INT, [_P, ctypes.c_uint64, ctypes.c_int32, _P, _U32, _P, _P, _P]),
+    "fdas_server_stats": (_INT, [_P, _P, _U32]),
+    "fdas_server_last_error": (ctypes.c_char_p, [_P]),
+    "fdas_server_destroy": (None, [_P]),
+    "fdas_batch_default_config": (None, [_P]),
+    "fdas_batch_create": (_INT, [_P, _P, _INT, _U32, _U32, _U32, _P, _P]),
+    "fdas_batch_set_inputs": (_INT, [_P, _P, _INT]),
+    "fdas_batch_input": (_P, [_P]),
+    "fdas_batch_run": (_INT, [_P, _P, _INT]),
+    "fdas_batch_wait": (_INT, [_P]),
+    "fdas_batch_trial": (_P, [_P, _U32]),
+    "fdas_batch_info": (_INT, [_P, _P, _U32, _P, _U32]),
+    "fdas_batch_set_tuning": (_INT, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "fdas_batch_last_error": (ctypes.c_char_p, [_P]),
+    "fdas_batch_destroy": (None, [_P]),
+    "fdas_reshape": (_INT, [_P, _U32, _U32, _U32, _U32, _U32]),
+    "fdas_series_to_spectrum": (_INT, [_P, _P, ctypes.c_uint64, _INT, ctypes.c_float, _P, _INT]),
     "fdas_ft_convolution_noalloc": (_INT, [_P, _U32, _P, _INT, _U32, _U32, _INT, _P, ctypes.c_uint64, _P, _P]),
     "fdas_version": (ctypes.c_char_p, []),
 }

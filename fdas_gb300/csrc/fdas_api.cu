@@ -65,6 +65,8 @@ struct BufferSet {
   bool have_templates = false;
   bool have_taps = false;
   bool have_input = false;
+  bool series_spectrum = false;  // d_input holds a spectrum made by fdas_series_to_spectrum
+  std::vector<int> taplen;       // non-zero taps per uploaded template row (host copy)
   bool fop_from_input = false;
   bool launched = false;
   bool ctrl_valid = false;
@@ -90,6 +92,12 @@ struct fdas_handle {
   void *log_user = nullptr;
   float2 *d_twiddle = nullptr;
   double2 *d_twiddle64 = nullptr;
+  float2 *d_series_tw = nullptr;  // e^(-i pi x / N), made on first use
+  // fdas_reshape: first template row in use, and the sizes the buffers were allocated for
+  int row0 = 0;
+  int rc_cap = kRecheckCap;  // entries of the near-threshold recheck list
+  int alloc_N = 0, alloc_T = 0, alloc_P = 0, alloc_tiles = 0;
+  size_t alloc_fop_floats = 0;
   BufferSet set[2];
   // print_stats bookkeeping
   float pipeline_accum_ms = 0.f;
@@ -225,15 +233,20 @@ fdas_status make_hsum_maps(fdas_handle *h, BufferSet &S) {
 // ---------------------------------------------------------------- stages
 fdas_status enqueue_input(fdas_handle *h, int ab, const fdas_complex *input, bool device_ptr) {
   BufferSet &S = h->set[ab];
-  if (!input) return fail(h, FDAS_ERR_INVALID_ARG, "input is NULL");
+  // NULL: the spectrum that fdas_series_to_spectrum left in this set
+  if (!input && !(S.series_spectrum && !device_ptr))
+    return fail(h, FDAS_ERR_INVALID_ARG, "input is NULL and no spectrum was made on this buffer set");
   CK(h, cudaEventRecord(S.ev[0], S.stream));
   if (h->cfg.sync_pipeline && h->set[1 - ab].ev_ftc_recorded)
     CK(h, cudaStreamWaitEvent(S.stream, h->set[1 - ab].ev[3], 0));  // FDAS.cpp:287-288
-  if (device_ptr) {
+  if (!input) {
+    S.cur_input = S.d_input;
+  } else if (device_ptr) {
     S.cur_input = reinterpret_cast<const float2 *>(input);
   } else {
     CK(h, cudaMemcpyAsync(S.d_input, input, sizeof(float2) * (size_t)h->N, cudaMemcpyHostToDevice, S.stream));
     S.cur_input = S.d_input;
+    S.series_spectrum = false;
   }
   CK(h, cudaEventRecord(S.ev[1], S.stream));
   S.have_input = true;
@@ -261,7 +274,7 @@ fdas_status enqueue_ftc(fdas_handle *h, int ab, fdas_fop_part which) {
   if (!S.have_input) return fail(h, FDAS_ERR_STATE, "no input tiled on this buffer set");
   FtcParams p{};
   p.tiles = S.d_tiles;
-  p.tmpl = S.d_tmpl;
+  p.tmpl = S.d_tmpl + (size_t)h->row0 * kTile;
   p.fop = S.d_fop;
   p.fop_stride = h->stride;
   p.n_bins = h->N;
@@ -324,7 +337,7 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   p.cand_cap = h->cap;
   p.rc_list = S.d_rc;
   p.rc_count = S.d_ctrl + kCtrlRecheckCount;
-  p.rc_cap = kRecheckCap;
+  p.rc_cap = h->rc_cap;
   p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlStatus);
   p.timeout_ns = 2000000000LL;  // 2 s
 
@@ -337,13 +350,13 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
     r.input = S.cur_input;
     r.n_bins = h->N;
     r.half = H;
-    r.taps = S.d_taps;
-    r.tap_len = S.d_taplen;
+    r.taps = S.d_taps + (size_t)h->row0 * h->tap_pitch;
+    r.tap_len = S.d_taplen + h->row0;
     r.tap_pitch = h->tap_pitch;
     for (int j = 0; j < kMaxPlanes; ++j) r.thr[j] = j < P ? (double)thr[j] : INFINITY;
     r.rc_list = S.d_rc;
     r.rc_count = S.d_ctrl + kCtrlRecheckCount;
-    r.rc_cap = kRecheckCap;
+    r.rc_cap = h->rc_cap;
     r.cand_key = S.d_key;
     r.cand_pwr = S.d_pwr;
     r.cand_total = S.d_ctrl + kCtrlTotal;
@@ -544,6 +557,11 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
   }
 
   const size_t fop_floats = (size_t)h->T * (size_t)h->stride + 4096;
+  h->alloc_N = h->N;
+  h->alloc_T = h->T;
+  h->alloc_P = h->P;
+  h->alloc_tiles = h->n_tiles;
+  h->alloc_fop_floats = fop_floats;
   for (int ab = 0; ab < 2; ++ab) {
     BufferSet &S = h->set[ab];
     struct A {
@@ -606,8 +624,59 @@ void fdas_destroy(fdas_handle *h) {
   for (auto &S : h->set) free_set(S);
   cudaFree(h->d_twiddle);
   cudaFree(h->d_twiddle64);
+  cudaFree(h->d_series_tw);
   if (h->pipeline_start) cudaEventDestroy(h->pipeline_start);
   delete h;
+}
+
+fdas_status fdas_reshape(fdas_handle *h, uint32_t n_frequency_bins, uint32_t template_row_begin,
+                         uint32_t n_templates, uint32_t tile_overlap, uint32_t n_planes) {
+  CHECK_HANDLE(h);
+  if (n_frequency_bins == 0 || n_frequency_bins > (uint32_t)h->alloc_N)
+    return fail(h, FDAS_ERR_INVALID_ARG, "n_frequency_bins must be 1 .. the initialised size");
+  if (n_templates == 0 || n_templates % 2 == 0 || template_row_begin + n_templates > (uint32_t)h->alloc_T)
+    return fail(h, FDAS_ERR_INVALID_ARG, "template rows must be an odd count within the initialised bank");
+  if (n_planes == 0 || n_planes > (uint32_t)h->alloc_P)
+    return fail(h, FDAS_ERR_INVALID_ARG, "n_planes must be 1 .. the initialised count");
+  // longest template of the range, from the uploaded banks
+  int longest = 0;
+  for (auto &S : h->set)
+    for (uint32_t r = template_row_begin; r < template_row_begin + n_templates && r < S.taplen.size(); ++r)
+      longest = std::max(longest, S.taplen[r]);
+  uint32_t O = tile_overlap ? tile_overlap : (longest > 0 ? ((uint32_t)longest - 1 + 3) / 4 * 4 : (uint32_t)h->O);
+  if (O >= (uint32_t)kTile) return fail(h, FDAS_ERR_INVALID_ARG, "tile_overlap must be < 2048");
+  if ((int)O + 1 < longest)
+    return fail(h, FDAS_ERR_INVALID_ARG, "tile_overlap is shorter than a template of the range (overlap-save)");
+  const int payload = kTile - (int)O;
+  const int n_tiles = ((int)n_frequency_bins + payload - 1) / payload;
+  const long long stride = ((long long)n_frequency_bins + kHsBins - 1) / kHsBins * kHsBins;
+  if (n_tiles > h->alloc_tiles || (size_t)n_templates * (size_t)stride + 4096 > h->alloc_fop_floats)
+    return fail(h, FDAS_ERR_CAPACITY, "shape does not fit the buffers the handle was initialised with");
+  for (auto &S : h->set)
+    if (S.pending) return fail(h, FDAS_ERR_STATE, "a buffer set holds a pending harmonic summing");
+  CK(h, cudaSetDevice(h->cfg.device));
+  for (auto &S : h->set) CK(h, cudaStreamSynchronize(S.stream));
+  h->N = (int)n_frequency_bins;
+  h->row0 = (int)template_row_begin;
+  h->T = (int)n_templates;
+  h->H = h->T / 2;
+  h->O = (int)O;
+  h->payload = payload;
+  h->n_tiles = n_tiles;
+  h->P = (int)n_planes;
+  h->stride = stride;
+  h->cfg.n_frequency_bins = n_frequency_bins;
+  h->cfg.n_templates = n_templates;
+  h->cfg.tile_overlap = O;
+  h->cfg.n_planes = n_planes;
+  for (auto &S : h->set) {
+    S.have_input = S.fop_from_input = S.launched = S.ctrl_valid = S.series_spectrum = false;
+    S.ev_ftc_recorded = false;
+    S.thresholds.clear();
+    fdas_status st = make_hsum_maps(h, S);
+    if (st != FDAS_OK) return st;
+  }
+  return FDAS_OK;
 }
 
 fdas_status fdas_upload_templates(fdas_handle *h, const fdas_complex *templates, fdas_template_layout layout,
@@ -618,10 +687,14 @@ fdas_status fdas_upload_templates(fdas_handle *h, const fdas_complex *templates,
   CK(h, cudaSetDevice(h->cfg.device));
   BufferSet &S = h->set[ab];
   const int T = h->T;
+  // rows [row0, row0 + T) of the set's template buffers (row0 = 0 unless reshaped)
+  float2 *d_tmpl = S.d_tmpl + (size_t)h->row0 * kTile;
+  double2 *d_taps = S.d_taps + (size_t)h->row0 * h->tap_pitch;
+  int *d_taplen = S.d_taplen + h->row0;
+  std::vector<int> len(T, 0);
   if (layout == FDAS_TEMPLATES_TIME_DOMAIN) {
     // ft_conv.py:203 convolves with the non-zero taps of each row
     std::vector<double2> taps((size_t)T * h->tap_pitch, make_double2(0.0, 0.0));
-    std::vector<int> len(T, 0);
     for (int r = 0; r < T; ++r) {
       int n = 0;
       for (int q = 0; q < h->L; ++q) {
@@ -632,15 +705,15 @@ fdas_status fdas_upload_templates(fdas_handle *h, const fdas_complex *templates,
         return fail(h, FDAS_ERR_INVALID_ARG, "template has more non-zero taps than tile_overlap + 1");
       len[r] = n;
     }
-    CK(h, cudaMemcpy(S.d_taps, taps.data(), sizeof(double2) * taps.size(), cudaMemcpyHostToDevice));
-    CK(h, cudaMemcpy(S.d_taplen, len.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(d_taps, taps.data(), sizeof(double2) * taps.size(), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(d_taplen, len.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     SpectraParams p{};
-    p.taps = S.d_taps;
-    p.tap_len = S.d_taplen;
+    p.taps = d_taps;
+    p.tap_len = d_taplen;
     p.tap_pitch = h->tap_pitch;
     p.n_templates = T;
     p.twiddle64 = h->d_twiddle64;
-    p.spectra = S.d_tmpl;
+    p.spectra = d_tmpl;
     CK(h, launch_spectra(p, S.stream));
     CK(h, cudaStreamSynchronize(S.stream));
   } else if (layout == FDAS_TEMPLATES_FFT_P4 || layout == FDAS_TEMPLATES_FFT_NATURAL) {
@@ -651,28 +724,31 @@ fdas_status fdas_upload_templates(fdas_handle *h, const fdas_complex *templates,
     }
     // unscaled spectra -> FP64 taps for the recheck (via the tiles buffer as scratch
     // would clash with a tiled input; use the template buffer before scaling)
-    CK(h, cudaMemcpy(S.d_tmpl, nat.data(), sizeof(float2) * nat.size(), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(d_tmpl, nat.data(), sizeof(float2) * nat.size(), cudaMemcpyHostToDevice));
     TapsParams tp{};
-    tp.spectra = S.d_tmpl;
+    tp.spectra = d_tmpl;
     tp.n_templates = T;
     tp.n_taps = h->O + 1;
     tp.twiddle64 = h->d_twiddle64;
-    tp.taps = S.d_taps;
-    tp.tap_len = S.d_taplen;
+    tp.taps = d_taps;
+    tp.tap_len = d_taplen;
     tp.tap_pitch = h->tap_pitch;
     CK(h, launch_taps(tp, S.stream));
     CK(h, cudaStreamSynchronize(S.stream));
+    CK(h, cudaMemcpy(len.data(), d_taplen, sizeof(int) * T, cudaMemcpyDeviceToHost));
     // 1/2048 of the inverse transform folded into the template spectra (exact)
     for (auto &c : nat) {
       c.re *= 1.0f / 2048.0f;
       c.im *= 1.0f / 2048.0f;
     }
-    CK(h, cudaMemcpy(S.d_tmpl, nat.data(), sizeof(float2) * nat.size(), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(d_tmpl, nat.data(), sizeof(float2) * nat.size(), cudaMemcpyHostToDevice));
   } else {
     return fail(h, FDAS_ERR_INVALID_ARG, "unknown template layout");
   }
   S.have_templates = true;
   S.have_taps = true;
+  if (S.taplen.size() < (size_t)h->alloc_T) S.taplen.assign(h->alloc_T, 0);
+  std::copy(len.begin(), len.end(), S.taplen.begin() + h->row0);
   logf(h, "[INFO] Uploaded template coefficients");
   return FDAS_OK;
 }
@@ -722,6 +798,43 @@ fdas_status fdas_perform_harmonic_summing(fdas_handle *h, const float *threshold
   if (st != FDAS_OK) return st;
   if ((st = sync_set(h, ab)) != FDAS_OK) return st;
   logf(h, "[INFO] Harmonic summing duration: %.3f ms", elapsed(S.ev[3], S.ev[4]));
+  return FDAS_OK;
+}
+
+fdas_status fdas_series_to_spectrum(fdas_handle *h, const float *samples, uint64_t n_samples, int samples_on_device,
+                                    float scale, fdas_complex *spectrum, fdas_buffer_set ab) {
+  CHECK_HANDLE(h);
+  CHECK_SET(h, ab);
+  if (!samples) return fail(h, FDAS_ERR_INVALID_ARG, "samples is NULL");
+  // ft_conv.py:125-132: at least 2 N samples; extra samples are ignored
+  if (n_samples < 2 * (uint64_t)h->N)
+    return fail(h, FDAS_ERR_INVALID_ARG, "the series needs at least 2 x n_frequency_bins samples");
+  int radix[64];
+  if (series_radices(h->N, radix, 64) < 0)
+    return fail(h, FDAS_ERR_UNSUPPORTED, "n_frequency_bins must factor into 2, 3, 5 and 7 for the series FFT");
+  BufferSet &S = h->set[ab];
+  if (S.pending)
+    return fail(h, FDAS_ERR_STATE, "buffer set holds a pending harmonic summing (sync_pipeline); end the pipeline first");
+  CK(h, cudaSetDevice(h->cfg.device));
+  if (!h->d_series_tw) {
+    CK(h, cudaMalloc(&h->d_series_tw, sizeof(float2) * (size_t)h->N));
+    CK(h, launch_series_twiddles(h->d_series_tw, h->N, S.stream));
+  }
+  CK(h, cudaMemcpyAsync(S.d_input, samples, sizeof(float) * 2 * (size_t)h->N,
+                        samples_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, S.stream));
+  SeriesParams p{};
+  p.z = S.d_input;
+  p.scratch = S.d_tiles;  // n_tiles x 2048 >= N complex
+  p.tw = h->d_series_tw;
+  p.n = h->N;
+  p.scale = scale;
+  CK(h, launch_series_spectrum(p, S.stream));
+  if (spectrum)
+    CK(h, cudaMemcpyAsync(spectrum, S.d_input, sizeof(float2) * (size_t)h->N, cudaMemcpyDeviceToHost, S.stream));
+  CK(h, cudaStreamSynchronize(S.stream));
+  S.series_spectrum = true;
+  S.have_input = false;  // the tiles buffer was used as scratch
+  logf(h, "[INFO] Spectrum of %llu samples -> %d bins", (unsigned long long)(2 * (uint64_t)h->N), h->N);
   return FDAS_OK;
 }
 
@@ -870,6 +983,11 @@ fdas_status fdas_retrieve_candidate_list(fdas_handle *h, fdas_candidate *out, ui
   uint32_t total = 0;
   for (int pl = 0; pl < h->P; ++pl) total += ctrl[kCtrlCount + pl];
   const uint32_t stored = std::min(ctrl[kCtrlTotal], (unsigned)h->cap);
+  if (capacity == 0) {  // counts only
+    if (n_total) *n_total = total;
+    if (n_dropped) *n_dropped = total - stored;
+    return FDAS_OK;
+  }
   std::vector<unsigned long long> keys(stored);
   std::vector<float> pwrs(stored);
   if (stored) {
@@ -1061,6 +1179,471 @@ fdas_status fdas_host_unregister(void *ptr) {
   cudaError_t e = cudaHostUnregister(ptr);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaHostUnregister", __FILE__, __LINE__);
   return FDAS_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched search (fdas_batch_*): many trials of uneven length in one pass.
+//
+// All trials' tiles are transformed by one tiling launch and all (trial, tile,
+// template) items by one persistent FT-convolution launch (the trial of a
+// global tile is found from a table of tile ranges), into one FOP arena with
+// each trial's FOP at its own offset.  Harmonic summing, FP64 recheck and
+// candidate selection then run per trial -- through "views", FDAS handles that
+// borrow the batch's buffers -- on a few branch streams.  The whole sequence
+// is captured once into a CUDA graph and replayed; before capture an
+// autotuner times the FFT split of the FT convolution (one warp, 64 x 32, or a
+// warp pair, 32 x 64), its CTAs per SM, and the harmonic-summing pipeline
+// depth on the batch itself and keeps the fastest.
+struct fdas_batch {
+  fdas_batch_config cfg{};
+  fdas_handle *owner = nullptr;  // holds the bank (spectra, FP64 taps) and the twiddle tables
+  int n_trials = 0;
+  int T = 0, O = 0, payload = 0, P = 0;
+  std::vector<BatchTrial> trials;
+  long long total_tiles = 0, total_bins = 0;
+  size_t fop_floats = 0;
+  float2 *d_input = nullptr, *d_tiles = nullptr;
+  float *d_fop = nullptr;
+  BatchTrial *d_trials = nullptr;
+  int *d_status = nullptr, *h_status = nullptr;
+  unsigned long long *d_key = nullptr, *d_sel_key = nullptr;
+  float *d_pwr = nullptr, *d_sel_pwr = nullptr, *d_cpwr = nullptr;
+  unsigned *d_ctrl = nullptr, *h_ctrl = nullptr, *d_hist = nullptr, *d_ticket = nullptr;
+  uint4 *d_rc = nullptr;
+  uint32_t *d_cloc = nullptr;
+  std::vector<fdas_handle *> views;
+  cudaStream_t main = nullptr;
+  std::vector<cudaStream_t> branch;
+  cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<float> graph_thr;
+  int ftc_variant = 2, ftc_ctas = 2, hsum_lean = 0;
+  bool tuned = false;
+  std::vector<float> tune_ms;
+  std::string err;
+};
+
+namespace {
+
+constexpr int kBatchBranches = 4;
+constexpr int kBatchRecheckCap = 8192;
+
+fdas_status bfail(fdas_batch *b, fdas_status st, const std::string &msg) {
+  if (b) b->err = msg;
+  else g_init_error = msg;
+  return st;
+}
+
+#define BCK(b, expr)                                                                        \
+  do {                                                                                      \
+    cudaError_t e_ = (expr);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      char m_[256];                                                                         \
+      snprintf(m_, sizeof(m_), "CUDA call failed with %s: %s", cudaGetErrorName(e_), #expr); \
+      return bfail((b), e_ == cudaErrorMemoryAllocation ? FDAS_ERR_OUT_OF_MEMORY : FDAS_ERR_CUDA, m_); \
+    }                                                                                       \
+  } while (0)
+
+void batch_free(fdas_batch *b) {
+  if (b->main) cudaStreamSynchronize(b->main);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (auto *v : b->views) {
+    for (auto &ev : v->set[0].ev)
+      if (ev) cudaEventDestroy(ev);
+    delete v;  // borrowed buffers: nothing else to free
+  }
+  void *dev[] = {b->d_input, b->d_tiles, b->d_fop, b->d_trials, b->d_status, b->d_key, b->d_sel_key, b->d_pwr,
+                 b->d_sel_pwr, b->d_cpwr, b->d_ctrl, b->d_hist, b->d_ticket, b->d_rc, b->d_cloc};
+  for (void *p : dev) cudaFree(p);
+  cudaFreeHost(b->h_ctrl);
+  cudaFreeHost(b->h_status);
+  for (auto s : b->branch) cudaStreamDestroy(s);
+  for (auto e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->t0) cudaEventDestroy(b->t0);
+  if (b->t1) cudaEventDestroy(b->t1);
+  if (b->main) cudaStreamDestroy(b->main);
+  if (b->owner) fdas_destroy(b->owner);
+  delete b;
+}
+
+// Enqueue the whole batched search on b->main (capturable).
+fdas_status batch_enqueue(fdas_batch *b, const float *thr) {
+  BCK(b, cudaMemsetAsync(b->d_status, 0, sizeof(int), b->main));
+  TileParams tp{};
+  tp.input = b->d_input;
+  tp.n_tiles = (int)b->total_tiles;
+  tp.overlap = b->O;
+  tp.payload = b->payload;
+  tp.tiles = b->d_tiles;
+  tp.twiddle = b->owner->d_twiddle;
+  tp.trials = b->d_trials;
+  tp.n_trials = b->n_trials;
+  BCK(b, launch_tile_fft(tp, b->main));
+  FtcParams fp{};
+  fp.tiles = b->d_tiles;
+  fp.tmpl = b->owner->set[0].d_tmpl;
+  fp.fop = b->d_fop;
+  fp.n_tiles = (int)b->total_tiles;
+  fp.overlap = b->O;
+  fp.payload = b->payload;
+  fp.row_begin = 0;
+  fp.n_rows = b->T;
+  fp.twiddle = b->owner->d_twiddle;
+  fp.status = b->d_status;
+  fp.timeout_ns = 2000000000LL;
+  fp.ctas_per_sm = b->ftc_ctas;
+  fp.variant = b->ftc_variant;
+  fp.trials = b->d_trials;
+  fp.n_trials = b->n_trials;
+  BCK(b, launch_ftc(fp, b->main));
+  BCK(b, cudaEventRecord(b->fork, b->main));
+  for (auto s : b->branch) BCK(b, cudaStreamWaitEvent(s, b->fork, 0));
+  for (int i = 0; i < b->n_trials; ++i) {
+    fdas_handle *v = b->views[i];
+    v->cfg.overlap = (uint32_t)b->hsum_lean;  // the lean harmonic-summing kernel
+    fdas_status st = enqueue_hsum(v, 0, thr, FDAS_ALL_ACCELERATIONS);
+    if (st != FDAS_OK) return bfail(b, st, v->err);
+  }
+  for (size_t k = 0; k < b->branch.size(); ++k) {
+    BCK(b, cudaEventRecord(b->joins[k], b->branch[k]));
+    BCK(b, cudaStreamWaitEvent(b->main, b->joins[k], 0));
+  }
+  BCK(b, cudaMemcpyAsync(b->h_status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, b->main));
+  return FDAS_OK;
+}
+
+fdas_status batch_capture(fdas_batch *b, const float *thr) {
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  BCK(b, cudaStreamBeginCapture(b->main, cudaStreamCaptureModeRelaxed));
+  fdas_status st = batch_enqueue(b, thr);
+  cudaError_t e = cudaStreamEndCapture(b->main, &g);
+  if (st != FDAS_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  BCK(b, e);
+  e = cudaGraphInstantiate(&b->exec, g, 0);
+  cudaGraphDestroy(g);
+  BCK(b, e);
+  b->graph_thr.assign(thr, thr + b->P);
+  return FDAS_OK;
+}
+
+// Time one configuration: two direct runs after a warm-up run.
+fdas_status batch_time(fdas_batch *b, const float *thr, float *ms) {
+  for (int rep = 0; rep < 3; ++rep) {
+    if (rep == 1) BCK(b, cudaEventRecord(b->t0, b->main));
+    fdas_status st = batch_enqueue(b, thr);
+    if (st != FDAS_OK) return st;
+  }
+  BCK(b, cudaEventRecord(b->t1, b->main));
+  BCK(b, cudaEventSynchronize(b->t1));
+  BCK(b, cudaEventElapsedTime(ms, b->t0, b->t1));
+  *ms *= 0.5f;
+  return FDAS_OK;
+}
+
+fdas_status batch_autotune(fdas_batch *b, const float *thr) {
+  struct Cfg {
+    int variant, ctas, lean;
+  };
+  const Cfg cands[] = {{2, 2, 0}, {2, 1, 0}, {1, 1, 0}, {2, 2, 1}, {2, 1, 1}, {1, 1, 1}};
+  float best = 1e30f;
+  Cfg pick = cands[0];
+  b->tune_ms.clear();
+  for (const Cfg &c : cands) {
+    b->ftc_variant = c.variant;
+    b->ftc_ctas = c.ctas;
+    b->hsum_lean = c.lean;
+    float ms = 0.f;
+    fdas_status st = batch_time(b, thr, &ms);
+    if (st != FDAS_OK) return st;
+    b->tune_ms.push_back(ms);
+    if (ms < best) {
+      best = ms;
+      pick = c;
+    }
+  }
+  b->ftc_variant = pick.variant;
+  b->ftc_ctas = pick.ctas;
+  b->hsum_lean = pick.lean;
+  b->tuned = true;
+  return FDAS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void fdas_batch_default_config(fdas_batch_config *c) {
+  std::memset(c, 0, sizeof(*c));
+  c->device = 0;
+  c->n_planes = 8;
+  c->candidate_capacity = 1u << 18;
+  c->candidates_per_plane_compat = 512;
+  c->autotune = 1;
+  c->recheck = 1;
+}
+
+fdas_status fdas_batch_create(const fdas_batch_config *cfg, const fdas_complex *bank, fdas_template_layout layout,
+                              uint32_t bank_rows, uint32_t bank_len, uint32_t n_trials, const uint32_t *n_bins,
+                              fdas_batch **out) {
+  if (!cfg || !bank || !n_bins || !out || n_trials == 0) return bfail(nullptr, FDAS_ERR_INVALID_ARG, "invalid argument");
+  if (cfg->n_planes == 0 || cfg->n_planes > (uint32_t)kMaxPlanes)
+    return bfail(nullptr, FDAS_ERR_INVALID_ARG, "n_planes must be 1..16");
+  for (uint32_t i = 0; i < n_trials; ++i)
+    if (n_bins[i] == 0) return bfail(nullptr, FDAS_ERR_INVALID_ARG, "a trial has no bins");
+  *out = nullptr;
+  fdas_batch *b = new fdas_batch();
+  b->cfg = *cfg;
+  fdas_config c;
+  fdas_default_config(&c, kTile);
+  c.device = cfg->device;
+  c.n_templates = bank_rows;
+  if (layout == FDAS_TEMPLATES_TIME_DOMAIN) c.max_template_len = bank_len;
+  c.n_planes = cfg->n_planes;
+  c.candidate_capacity = 1024;
+  c.recheck = cfg->recheck;
+  fdas_status st = fdas_initialise_accelerator(&c, &b->owner);
+  if (st != FDAS_OK) {
+    delete b;
+    return st;
+  }
+  if ((st = fdas_upload_templates(b->owner, bank, layout, FDAS_SET_A)) != FDAS_OK) {
+    g_init_error = b->owner->err;
+    batch_free(b);
+    return st;
+  }
+  fdas_handle *o = b->owner;
+  b->n_trials = (int)n_trials;
+  b->T = o->T;
+  b->O = o->O;
+  b->payload = o->payload;
+  b->P = o->P;
+  const int cap = (int)(cfg->candidate_capacity ? cfg->candidate_capacity : (1u << 18));
+  const int per_plane = (int)(cfg->candidates_per_plane_compat ? cfg->candidates_per_plane_compat : 512);
+  if (per_plane > kMaxCompat) {
+    batch_free(b);
+    return bfail(nullptr, FDAS_ERR_INVALID_ARG, "candidates_per_plane_compat must be <= 2048");
+  }
+  // trial table: tile ranges, input and FOP offsets (FOP rows 256-float aligned)
+  b->trials.resize(n_trials);
+  long long tile = 0, in = 0;
+  size_t fop = 0;
+  for (uint32_t i = 0; i < n_trials; ++i) {
+    BatchTrial &t = b->trials[i];
+    t.tile_begin = tile;
+    t.input_offset = in;
+    t.fop_offset = (long long)fop;
+    t.stride = ((long long)n_bins[i] + kHsBins - 1) / kHsBins * kHsBins;
+    t.n_bins = (int)n_bins[i];
+    t.pad_ = 0;
+    tile += ((long long)n_bins[i] + b->payload - 1) / b->payload;
+    in += n_bins[i];
+    fop += (size_t)b->T * (size_t)t.stride;
+  }
+  b->total_tiles = tile;
+  b->total_bins = in;
+  b->fop_floats = fop + 4096;
+  if ((long long)b->total_tiles * b->T >= (1ll << 31)) {
+    batch_free(b);
+    return bfail(nullptr, FDAS_ERR_CAPACITY, "too many (tile, template) items for one batch");
+  }
+  const size_t n = n_trials;
+  const size_t P = (size_t)b->P;
+#define BALLOC(ptr, bytes)                                                          \
+  if (cudaMalloc((void **)&(ptr), (bytes)) != cudaSuccess) {                         \
+    cudaGetLastError();                                                             \
+    batch_free(b);                                                                  \
+    return bfail(nullptr, FDAS_ERR_OUT_OF_MEMORY, "batch device allocation failed"); \
+  }
+  BALLOC(b->d_input, sizeof(float2) * (size_t)(b->total_bins + 64));
+  BALLOC(b->d_tiles, sizeof(float2) * (size_t)b->total_tiles * kTile);
+  BALLOC(b->d_fop, sizeof(float) * b->fop_floats);
+  BALLOC(b->d_trials, sizeof(BatchTrial) * n);
+  BALLOC(b->d_status, sizeof(int));
+  BALLOC(b->d_key, sizeof(unsigned long long) * n * cap);
+  BALLOC(b->d_pwr, sizeof(float) * n * cap);
+  BALLOC(b->d_ctrl, sizeof(unsigned) * n * kCtrlWords);
+  BALLOC(b->d_rc, sizeof(uint4) * n * kBatchRecheckCap);
+  BALLOC(b->d_hist, sizeof(unsigned) * n * P * kSelBuckets);
+  BALLOC(b->d_ticket, sizeof(unsigned) * n);
+  BALLOC(b->d_sel_key, sizeof(unsigned long long) * n * P * 2 * kSortCap);
+  BALLOC(b->d_sel_pwr, sizeof(float) * n * P * 2 * kSortCap);
+  BALLOC(b->d_cloc, sizeof(uint32_t) * n * P * per_plane);
+  BALLOC(b->d_cpwr, sizeof(float) * n * P * per_plane);
+#undef BALLOC
+  cudaError_t e;
+  if ((e = cudaMemcpy(b->d_trials, b->trials.data(), sizeof(BatchTrial) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemset(b->d_fop, 0, sizeof(float) * b->fop_floats)) != cudaSuccess ||
+      (e = cudaMemset(b->d_hist, 0, sizeof(unsigned) * n * P * kSelBuckets)) != cudaSuccess ||
+      (e = cudaMemset(b->d_ticket, 0, sizeof(unsigned) * n)) != cudaSuccess ||
+      (e = cudaMemset(b->d_ctrl, 0, sizeof(unsigned) * n * kCtrlWords)) != cudaSuccess ||
+      (e = cudaHostAlloc((void **)&b->h_ctrl, sizeof(unsigned) * n * kCtrlWords, cudaHostAllocDefault)) != cudaSuccess ||
+      (e = cudaHostAlloc((void **)&b->h_status, sizeof(int), cudaHostAllocDefault)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreate(&b->t0)) != cudaSuccess || (e = cudaEventCreate(&b->t1)) != cudaSuccess) {
+    batch_free(b);
+    return bfail(nullptr, FDAS_ERR_CUDA, std::string("batch setup: ") + cudaGetErrorString(e));
+  }
+  *b->h_status = 0;
+  for (int k = 0; k < kBatchBranches; ++k) {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      batch_free(b);
+      return bfail(nullptr, FDAS_ERR_CUDA, "batch streams");
+    }
+    b->branch.push_back(s);
+    b->joins.push_back(ev);
+  }
+  // views: one handle per trial over the batch buffers
+  const BufferSet &OS = o->set[0];
+  for (uint32_t i = 0; i < n_trials; ++i) {
+    const BatchTrial &t = b->trials[i];
+    fdas_handle *v = new fdas_handle();
+    b->views.push_back(v);
+    v->cfg = o->cfg;
+    v->cfg.n_frequency_bins = (uint32_t)t.n_bins;
+    v->cfg.candidate_capacity = (uint32_t)cap;
+    v->cfg.candidates_per_plane_compat = (uint32_t)per_plane;
+    v->N = t.n_bins;
+    v->T = o->T;
+    v->H = o->H;
+    v->L = o->L;
+    v->O = o->O;
+    v->payload = o->payload;
+    v->n_tiles = (int)(((long long)t.n_bins + o->payload - 1) / o->payload);
+    v->P = o->P;
+    v->cap = cap;
+    v->per_plane = per_plane;
+    v->stride = t.stride;
+    v->tap_pitch = o->tap_pitch;
+    v->rc_cap = kBatchRecheckCap;
+    v->d_twiddle = o->d_twiddle;
+    v->d_twiddle64 = o->d_twiddle64;
+    v->alloc_N = v->N;
+    v->alloc_T = v->T;
+    v->alloc_P = v->P;
+    v->alloc_tiles = v->n_tiles;
+    BufferSet &S = v->set[0];
+    S.stream = b->branch[i % kBatchBranches];
+    S.d_input = b->d_input + t.input_offset;
+    S.cur_input = S.d_input;
+    S.d_tiles = b->d_tiles + (size_t)t.tile_begin * kTile;
+    S.d_tmpl = OS.d_tmpl;
+    S.d_taps = OS.d_taps;
+    S.d_taplen = OS.d_taplen;
+    S.taplen = OS.taplen;
+    S.d_fop = b->d_fop + t.fop_offset;
+    S.d_key = b->d_key + (size_t)i * cap;
+    S.d_pwr = b->d_pwr + (size_t)i * cap;
+    S.d_ctrl = b->d_ctrl + (size_t)i * kCtrlWords;
+    S.h_ctrl = b->h_ctrl + (size_t)i * kCtrlWords;
+    S.d_rc = b->d_rc + (size_t)i * kBatchRecheckCap;
+    S.d_hist = b->d_hist + (size_t)i * P * kSelBuckets;
+    S.d_ticket = b->d_ticket + i;
+    S.d_sel_key = b->d_sel_key + (size_t)i * P * 2 * kSortCap;
+    S.d_sel_pwr = b->d_sel_pwr + (size_t)i * P * 2 * kSortCap;
+    S.d_cloc = b->d_cloc + (size_t)i * P * per_plane;
+    S.d_cpwr = b->d_cpwr + (size_t)i * P * per_plane;
+    S.have_templates = S.have_taps = S.have_input = S.fop_from_input = true;
+    for (auto &ev : S.ev)
+      if (cudaEventCreate(&ev) != cudaSuccess) {
+        batch_free(b);
+        return bfail(nullptr, FDAS_ERR_CUDA, "batch events");
+      }
+    if ((st = make_hsum_maps(v, S)) != FDAS_OK) {
+      g_init_error = v->err;
+      batch_free(b);
+      return st;
+    }
+  }
+  *out = b;
+  return FDAS_OK;
+}
+
+fdas_status fdas_batch_set_inputs(fdas_batch *b, const fdas_complex *spectra, int on_device) {
+  if (!b || !spectra) return bfail(b, FDAS_ERR_INVALID_ARG, "spectra is NULL");
+  BCK(b, cudaSetDevice(b->cfg.device));
+  BCK(b, cudaMemcpyAsync(b->d_input, spectra, sizeof(float2) * (size_t)b->total_bins,
+                         on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->main));
+  return FDAS_OK;
+}
+
+fdas_complex *fdas_batch_input(fdas_batch *b) { return b ? reinterpret_cast<fdas_complex *>(b->d_input) : nullptr; }
+
+fdas_status fdas_batch_run(fdas_batch *b, const float *thresholds, int wait) {
+  if (!b || !thresholds) return bfail(b, FDAS_ERR_INVALID_ARG, "thresholds is NULL");
+  BCK(b, cudaSetDevice(b->cfg.device));
+  const bool same = b->exec && std::equal(thresholds, thresholds + b->P, b->graph_thr.begin());
+  if (!same) {
+    if (b->cfg.autotune && !b->tuned) {
+      fdas_status st = batch_autotune(b, thresholds);
+      if (st != FDAS_OK) return st;
+    }
+    fdas_status st = batch_capture(b, thresholds);
+    if (st != FDAS_OK) return st;
+  }
+  BCK(b, cudaGraphLaunch(b->exec, b->main));
+  for (auto *v : b->views) v->set[0].launched = true;
+  if (!wait) return FDAS_OK;
+  return fdas_batch_wait(b);
+}
+
+fdas_status fdas_batch_wait(fdas_batch *b) {
+  if (!b) return bfail(b, FDAS_ERR_INVALID_ARG, "null batch");
+  BCK(b, cudaStreamSynchronize(b->main));
+  if (*b->h_status & kStatusFtcTimeout) return bfail(b, FDAS_ERR_TIMEOUT, "FT convolution wait timed out");
+  for (auto *v : b->views)
+    if (v->set[0].h_ctrl[kCtrlStatus] & kStatusHsumTimeout)
+      return bfail(b, FDAS_ERR_TIMEOUT, "harmonic summing: shared-memory staging timed out");
+  return FDAS_OK;
+}
+
+fdas_handle *fdas_batch_trial(fdas_batch *b, uint32_t trial) {
+  return (b && trial < (uint32_t)b->n_trials) ? b->views[trial] : nullptr;
+}
+
+fdas_status fdas_batch_info(fdas_batch *b, int32_t *out, uint32_t n, float *tune_ms, uint32_t n_ms) {
+  if (!b) return FDAS_ERR_INVALID_ARG;
+  const int32_t v[6] = {b->ftc_variant, b->ftc_ctas, b->hsum_lean, b->tuned ? 1 : 0, (int32_t)b->total_tiles,
+                        (int32_t)b->tune_ms.size()};
+  for (uint32_t i = 0; out && i < n && i < 6; ++i) out[i] = v[i];
+  for (uint32_t i = 0; tune_ms && i < n_ms && i < b->tune_ms.size(); ++i) tune_ms[i] = b->tune_ms[i];
+  return FDAS_OK;
+}
+
+fdas_status fdas_batch_set_tuning(fdas_batch *b, int32_t ftc_variant, int32_t ftc_ctas_per_sm, int32_t hsum_lean) {
+  if (!b || ftc_variant < 1 || ftc_variant > 2 || ftc_ctas_per_sm < 1 || ftc_ctas_per_sm > 2)
+    return bfail(b, FDAS_ERR_INVALID_ARG, "invalid tuning");
+  b->ftc_variant = ftc_variant;
+  b->ftc_ctas = ftc_ctas_per_sm;
+  b->hsum_lean = hsum_lean ? 1 : 0;
+  b->tuned = true;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  return FDAS_OK;
+}
+
+const char *fdas_batch_last_error(const fdas_batch *b) { return b ? b->err.c_str() : g_init_error.c_str(); }
+
+void fdas_batch_destroy(fdas_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->cfg.device);
+  batch_free(b);
 }
 
 }  // extern "C"

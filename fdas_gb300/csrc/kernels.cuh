@@ -28,6 +28,29 @@ __host__ __device__ inline unsigned long long cand_key(int plane, int row, int b
 }
 
 // ---- (a) overlap-save tiling + forward FFT (tile_input.cl.mako, fft_4p.cl)
+// One trial of a batched search: its tiles are the global tiles
+// [tile_begin, next trial's tile_begin), its spectrum starts at input_offset of
+// the batch input, its FOP (n_templates rows of `stride` floats) at fop_offset.
+struct BatchTrial {
+  long long tile_begin;
+  long long input_offset;
+  long long fop_offset;
+  long long stride;
+  int n_bins;
+  int pad_;
+};
+
+// trial of global tile `tile` (trials sorted by tile_begin; binary search)
+__device__ __forceinline__ int batch_trial_of(const BatchTrial *tr, int n, long long tile) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tr[mid].tile_begin <= tile) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 struct TileParams {
   const float2 *input;    // N spectrum bins
   int n_bins;
@@ -36,6 +59,8 @@ struct TileParams {
   int payload;            // P = 2048 - O
   float2 *tiles;          // n_tiles x 2048, natural bin order
   const float2 *twiddle;  // e^(+2 pi i j / 2048), j < 2048
+  const BatchTrial *trials = nullptr;  // batched search: n_tiles spans all trials
+  int n_trials = 0;
 };
 
 // ---- (c) template multiply + inverse FFT + |.|^2 + discard (mux_and_mult,
@@ -55,6 +80,9 @@ struct FtcParams {
   int *status;
   long long timeout_ns;
   int ctas_per_sm;        // persistent CTAs per SM (1 leaves room for harmonic summing)
+  int variant = 0;        // FFT split: 0 default, 1 one warp per item (64 x 32), 2 a warp pair (32 x 64)
+  const BatchTrial *trials = nullptr;  // batched search: tiles of all trials, FOPs per trial
+  int n_trials = 0;
 };
 
 // ---- (d) harmonic summing + thresholds + candidate compaction (preload,
@@ -156,6 +184,19 @@ struct TapsParams {
   int *tap_len;
   int tap_pitch;
 };
+
+// ---- upstream: spectrum of a real series (ft_conv.py:134-143)
+struct SeriesParams {
+  float2 *z;              // N complex: the 2N samples on entry, the N-bin spectrum on exit
+  float2 *scratch;        // N complex
+  const float2 *tw;       // e^(-i pi x / N), x < N
+  int n;                  // N
+  float scale;            // applied to every output bin (1 / (2N) in ft_conv.py)
+};
+// radix sequence of an N-point mixed-radix FFT (8, 4, 2, 3, 5, 7); -1 if N has another factor
+int series_radices(int n, int *radix, int max_passes);
+cudaError_t launch_series_twiddles(float2 *tw, int n, cudaStream_t s);
+cudaError_t launch_series_spectrum(const SeriesParams &p, cudaStream_t s);
 
 cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s);
 cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s);

@@ -21,13 +21,22 @@ __global__ void __launch_bounds__(256) tile_fft_kernel(TileParams p) {
   float *ex = reinterpret_cast<float *>(smem_f4) + warp * kExFloats;
   const TwiddleBases tb = load_twiddle_bases<-1>(p.twiddle, lane);
   float2 v[64];
-  const long long start = (long long)tile * p.payload - p.overlap;
+  const float2 *input = p.input;
+  int n_bins = p.n_bins;
+  long long local = tile;
+  if (p.trials) {  // batched: the trial's own spectrum and tile numbering
+    const BatchTrial &tr = p.trials[batch_trial_of(p.trials, p.n_trials, tile)];
+    input += tr.input_offset;
+    n_bins = tr.n_bins;
+    local = tile - tr.tile_begin;
+  }
+  const long long start = local * p.payload - p.overlap;
   sfor<2>([&](auto C) {
     constexpr int c = decltype(C)::value;
     sfor<32>([&](auto D) {
       constexpr int d = decltype(D)::value;
       const long long b = start + lane + 32 * c + 64 * d;
-      v[32 * c + d] = (b >= 0 && b < p.n_bins) ? __ldg(p.input + b) : make_float2(0.f, 0.f);
+      v[32 * c + d] = (b >= 0 && b < n_bins) ? __ldg(input + b) : make_float2(0.f, 0.f);
     });
   });
   fft2048_core(v, tb, ex, lane);
@@ -81,6 +90,21 @@ __device__ __forceinline__ void prefetch_template(float *ex, const float2 *src, 
           smem_addr(ex)),
       "l"(src), "r"((uint32_t)(kTile * 8)), "r"(smem_addr(bar))
       : "memory");
+}
+
+// Where the outputs of (global tile, FOP row) go: the row's start, the bin of
+// the tile's first output (before the discard) and the row length.
+struct FopTarget {
+  float *out;
+  long long base;
+  int n_bins;
+};
+__device__ __forceinline__ FopTarget fop_target(const FtcParams &p, int tile, int row) {
+  if (!p.trials)
+    return FopTarget{p.fop + (long long)row * p.fop_stride, (long long)tile * p.payload - p.overlap, p.n_bins};
+  const BatchTrial &tr = p.trials[batch_trial_of(p.trials, p.n_trials, tile)];
+  return FopTarget{p.fop + tr.fop_offset + (long long)row * tr.stride,
+                   (tile - tr.tile_begin) * p.payload - p.overlap, tr.n_bins};
 }
 
 // Persistent: one CTA of 8 warps per SM; each warp loops over (tile,
@@ -137,16 +161,15 @@ __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
       if (next < n_items && lane == 0)
         prefetch_template(ex, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
     });
-    float *out = p.fop + (long long)row * p.fop_stride;
-    const long long base = (long long)tile * p.payload - p.overlap;
+    const FopTarget tg = fop_target(p, tile, row);
     sfor<2>([&](auto C) {
       constexpr int c = decltype(C)::value;
       sfor<32>([&](auto D) {
         constexpr int d = decltype(D)::value;
         const int n = lane + 32 * c + 64 * d;
-        const long long b = base + n;
+        const long long b = tg.base + n;
         const float2 y = v[32 * c + pos32(d)];
-        if (n >= p.overlap && b < p.n_bins) out[b] = fmaf(y.x, y.x, y.y * y.y);
+        if (n >= p.overlap && b < tg.n_bins) tg.out[b] = fmaf(y.x, y.x, y.y * y.y);
       });
     });
   }
@@ -231,15 +254,14 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
       if (next < n_items && tp == 0)
         prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
     });
-    float *out = p.fop + (long long)row * p.fop_stride;
-    const long long base = (long long)tile * p.payload - p.overlap;
+    const FopTarget tg = fop_target(p, tile, row);
     sfor<4>([&](auto R) {
       constexpr int r = decltype(R)::value;
       sfor<8>([&](auto D2) {
         constexpr int d2 = decltype(D2)::value;
         const int n = m + 32 * (4 * g + r) + 256 * d2;
-        const long long b = base + n;
-        if (n >= p.overlap && b < p.n_bins) out[b] = pw[8 * r + d2];
+        const long long b = tg.base + n;
+        if (n >= p.overlap && b < tg.n_bins) tg.out[b] = pw[8 * r + d2];
       });
     });
   }
@@ -317,7 +339,7 @@ cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
     if (n_sm <= 0) n_sm = 1;
   }
   const long long items = (long long)p.n_tiles * p.n_rows;
-  if (ftc_variant() == 1) {
+  if ((p.variant ? p.variant : ftc_variant()) == 1) {
     const int smem = ex_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(ftc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;

@@ -49,6 +49,15 @@ class FDAS:
         self.last_error = ""
         self._log_cb = _lib.LOG_FN(self._on_log)
         self.config = None
+        self._borrowed = False
+
+    @classmethod
+    def view(cls, handle, log=None):
+        """An FDAS over a handle owned elsewhere (a trial of a batch); never destroyed here."""
+        f = cls(log)
+        f._h = ctypes.c_void_p(handle)
+        f._borrowed = True
+        return f
 
     # ----------------------------------------------------------- plumbing
     def _on_log(self, line, _user):
@@ -68,7 +77,7 @@ class FDAS:
 
     def __del__(self):
         try:
-            if self._h:
+            if self._h and not self._borrowed:
                 self._lib.fdas_destroy(self._h)
                 self._h = ctypes.c_void_p()
         except Exception:
@@ -108,6 +117,15 @@ class FDAS:
         self.config = cfg
         return True
 
+    def reshape(self, n_frequency_bins, template_row_begin=0, n_templates=None, tile_overlap=0, n_planes=None):
+        """Re-size the idle handle within its initialised sizes (fdas_reshape):
+        fewer bins, a contiguous odd range of the uploaded bank's rows (the
+        z = -21..+21 half bank is rows 21..63 of the 85-row bank), fewer planes."""
+        n_templates = self.config.n_templates if n_templates is None else n_templates
+        n_planes = self.config.n_planes if n_planes is None else n_planes
+        return self._check(self._lib.fdas_reshape(self._h, int(n_frequency_bins), int(template_row_begin),
+                                                  int(n_templates), int(tile_overlap), int(n_planes)), "reshape")
+
     def upload_templates(self, templates, ab, layout=None):
         """FDAS::upload_templates.  ``templates`` complex64, n_templates x 2048
         spectra in p4 FFT order (the reference's ``..._ft_p4.npy``) unless
@@ -125,8 +143,30 @@ class FDAS:
         return self._check(self._lib.fdas_upload_thresholds(self._h, _ptr(thr), int(ab)), "upload_thresholds")
 
     def perform_input_tiling(self, input, ab):
-        x = _require(np.ascontiguousarray(input), np.complex64, self.get_input_sz(), "input")
+        """``input`` None: tile the spectrum series_to_spectrum made on ``ab``."""
+        x = None if input is None else _require(np.ascontiguousarray(input), np.complex64, self.get_input_sz(),
+                                                "input")
         return self._check(self._lib.fdas_perform_input_tiling(self._h, _ptr(x), int(ab)), "perform_input_tiling")
+
+    def series_to_spectrum(self, samples, ab, scale=None, spectrum=None):
+        """Upstream step of ft_conv.py:134-143 on the GPU: the N-bin spectrum of
+        the first 2N samples, ``fft(samples) * scale`` with the reference's
+        ``scale = 1 / (2N)`` by default.  ``samples`` is a float32 numpy array or
+        a CUDA tensor (anything with ``data_ptr()``).  The spectrum stays on
+        buffer set ``ab`` for perform_input_tiling / launch with input None and
+        is copied into ``spectrum`` (complex64[N]) when given."""
+        n = self.get_input_sz()
+        scale = 1.0 / (2 * n) if scale is None else float(scale)
+        out = None if spectrum is None else _require(spectrum, np.complex64, n, "spectrum")
+        if hasattr(samples, "data_ptr"):
+            if samples.dtype.__str__() != "torch.float32" or not samples.is_cuda or not samples.is_contiguous():
+                raise TypeError("samples must be a contiguous float32 CUDA tensor")
+            ptr, count, on_dev = ctypes.c_void_p(samples.data_ptr()), samples.numel(), 1
+        else:
+            x = _require(np.ascontiguousarray(samples), np.float32, None, "samples")
+            ptr, count, on_dev = _ptr(x), x.size, 0
+        return self._check(self._lib.fdas_series_to_spectrum(self._h, ptr, count, on_dev, scale, _ptr(out), int(ab)),
+                           "series_to_spectrum")
 
     def perform_ft_convolution(self, which, ab):
         return self._check(self._lib.fdas_perform_ft_convolution(self._h, int(which), int(ab)),
@@ -142,7 +182,7 @@ class FDAS:
 
     def launch(self, input, thresholds, detection_location, detection_power, which, ab):
         """FDAS::launch: asynchronous; the arrays must stay alive until wait()."""
-        x = _require(input, np.complex64, self.get_input_sz(), "input")
+        x = None if input is None else _require(input, np.complex64, self.get_input_sz(), "input")
         thr = None
         if thresholds is not None:
             thr = _require(np.ascontiguousarray(thresholds, dtype=np.float32), np.float32,
@@ -215,10 +255,14 @@ class FDAS:
 
         Returns (records, n_total, n_dropped); records has fields harmonic,
         template_num, bin, power."""
-        if capacity is None:
-            capacity = self.config.candidate_capacity or (1 << 22)
-        out = np.zeros(capacity, dtype=self.CANDIDATE_DTYPE)
         n_total, n_dropped = ctypes.c_uint32(), ctypes.c_uint32()
+        if capacity is None:  # exactly the stored records
+            if not self._check(self._lib.fdas_retrieve_candidate_list(self._h, None, 0, ctypes.byref(n_total),
+                                                                      ctypes.byref(n_dropped), int(ab)),
+                               "retrieve_candidate_list"):
+                return None, 0, 0
+            capacity = int(n_total.value) - int(n_dropped.value)
+        out = np.zeros(capacity, dtype=self.CANDIDATE_DTYPE)
         ok = self._check(self._lib.fdas_retrieve_candidate_list(self._h, _ptr(out), capacity, ctypes.byref(n_total),
                                                                 ctypes.byref(n_dropped), int(ab)),
                          "retrieve_candidate_list")

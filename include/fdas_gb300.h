@@ -114,6 +114,18 @@ void fdas_destroy(fdas_handle *h);
 /* Last error message of `h` (or of the last failed initialisation if h is NULL). */
 const char *fdas_last_error(const fdas_handle *h);
 
+/* Re-size an idle handle within the sizes it was initialised with (no
+ * counterpart in the reference; lets one handle serve searches of different
+ * lengths and banks without reallocating): N' <= N bins, the template rows
+ * [template_row_begin, template_row_begin + n_templates) of the uploaded bank
+ * (an odd count; 21 + 43 rows of the 85-row bank is the z = -21..+21 half
+ * bank), n_planes' <= n_planes, and tile_overlap (0 = from the longest
+ * template of the range).  Template spectra stay on the device; uploaded
+ * thresholds, inputs and FOP contents are dropped.  FDAS_ERR_CAPACITY if the
+ * tiles or the FOP of the new shape do not fit. */
+fdas_status fdas_reshape(fdas_handle *h, uint32_t n_frequency_bins, uint32_t template_row_begin,
+                         uint32_t n_templates, uint32_t tile_overlap, uint32_t n_planes);
+
 /* FDAS::upload_templates (FDAS.h:51, FDAS.cpp:263-269).  `templates` is a host
  * array of n_templates x 2048 complex values (FFT layouts) or n_templates x
  * max_template_len taps (FDAS_TEMPLATES_TIME_DOMAIN).  Blocking. */
@@ -126,6 +138,7 @@ fdas_status fdas_upload_thresholds(fdas_handle *h, const float *thresholds, fdas
 
 /* FDAS::perform_input_tiling (FDAS.h:55, FDAS.cpp:319-328): copy the N-bin
  * spectrum to the device, build the overlap-save tiles and transform them.
+ * `input` NULL: use the spectrum fdas_series_to_spectrum made on this set.
  * Blocking. */
 fdas_status fdas_perform_input_tiling(fdas_handle *h, const fdas_complex *input, fdas_buffer_set ab);
 
@@ -141,7 +154,8 @@ fdas_status fdas_perform_harmonic_summing(fdas_handle *h, const float *threshold
 /* FDAS::launch (FDAS.h:61, FDAS.cpp:548-583): enqueue tiling, FT convolution,
  * harmonic summing and the candidate download into the caller's
  * `detection_location` / `detection_power` (get_candidate_list_sz() entries
- * each).  Returns without waiting; use fdas_wait. */
+ * each).  `input` NULL: search the spectrum fdas_series_to_spectrum made on
+ * this set.  Returns without waiting; use fdas_wait. */
 fdas_status fdas_launch(fdas_handle *h, const fdas_complex *input, const float *thresholds,
                         uint32_t *detection_location, float *detection_power, fdas_fop_part which,
                         fdas_buffer_set ab);
@@ -231,6 +245,19 @@ void fdas_host_free(void *ptr);
 fdas_status fdas_host_register(void *ptr, size_t bytes);
 fdas_status fdas_host_unregister(void *ptr);
 
+/* Upstream step (ft_conv.py:134-143; no method of the reference's FDAS class):
+ * the spectrum X[k] = scale * sum_n x[n] e^(-2 pi i n k / 2N), k < N, of the
+ * first 2N samples of a real float32 series, N = n_frequency_bins.  The
+ * reference's test-data script uses scale = 1 / (2N) (`fft(samples) / n_samp`)
+ * and needs n_samples >= 2N (ft_conv.py:125-132).  `samples` is host memory,
+ * or device memory when samples_on_device != 0.  The spectrum is left in the
+ * set's input buffer -- fdas_perform_input_tiling / fdas_launch with input NULL
+ * search it -- and, when `spectrum` is not NULL, copied to that host array of N
+ * values.  N must factor into 2, 3, 5 and 7 (else FDAS_ERR_UNSUPPORTED).
+ * Blocking. */
+fdas_status fdas_series_to_spectrum(fdas_handle *h, const float *samples, uint64_t n_samples, int samples_on_device,
+                                    float scale, fdas_complex *spectrum, fdas_buffer_set ab);
+
 /* ------------------------------------------------------------------------
  * Device-resident entry points (no counterpart in the reference).  They let a
  * caller whose spectrum already sits in device memory run the same pipeline
@@ -299,6 +326,105 @@ fdas_status fdas_ft_convolution_noalloc(const fdas_complex *d_spectrum, uint32_t
                                         const fdas_complex *d_templates, fdas_template_layout layout,
                                         uint32_t n_templates, uint32_t tile_overlap, fdas_fop_part which,
                                         float *d_fop, uint64_t fop_stride, int32_t *d_status, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Request server (no counterpart in the reference; the served form of the
+ * search).  One dispatcher thread runs queued requests on a pool of slots --
+ * FDAS handles of power-of-two length classes with the template bank resident
+ * on the device, reshaped per request -- each on its own stream, so requests
+ * overlap on the device.  A request is admitted when a free slot of its class
+ * exists or a new slot's device bytes (mostly its FOPs: 4 x templates x bins
+ * per buffer set) fit the HBM budget; idle slots are released to make room.
+ * A request's result does not depend on the other requests in flight.
+ * ---------------------------------------------------------------------- */
+typedef struct fdas_server fdas_server;
+typedef struct {
+  int32_t device;
+  uint32_t max_bins;           /* longest request (2^21) */
+  uint32_t min_class_bins;     /* smallest slot length class (2^15) */
+  uint32_t max_planes;         /* planes a request may ask for, <= 16 */
+  uint32_t max_slots;          /* searches in flight at most */
+  uint64_t hbm_budget_bytes;   /* device bytes for slots; 0 = 90% of free HBM at creation */
+  uint32_t candidate_capacity; /* hit records per slot (2^20) */
+} fdas_server_config;
+
+void fdas_server_default_config(fdas_server_config *cfg);
+/* `bank`: bank_rows templates in `layout` (bank_len taps per row for
+ * FDAS_TEMPLATES_TIME_DOMAIN, 2048 spectrum values otherwise). */
+fdas_status fdas_server_create(const fdas_server_config *cfg, const fdas_complex *bank, fdas_template_layout layout,
+                               uint32_t bank_rows, uint32_t bank_len, fdas_server **out);
+/* Queue one search: n_bins spectrum values (copied), the bank rows
+ * [template_row_begin, template_row_begin + n_templates) (odd count), n_planes
+ * thresholds.  Returns at once with the request's id. */
+fdas_status fdas_server_submit(fdas_server *s, const fdas_complex *spectrum, uint32_t n_bins,
+                               uint32_t template_row_begin, uint32_t n_templates, uint32_t n_planes,
+                               const float *thresholds, uint64_t *request_id);
+/* Wait up to timeout_ms (< 0: no limit; FDAS_ERR_TIMEOUT when it runs out)
+ * for a request and collect its result: up to `capacity` wide candidate
+ * records in the order of fdas_retrieve_candidate_list, the hit count, the
+ * hits lost to the slot's capacity, and the submit-to-result latency.  A
+ * collected request is forgotten, except when out is NULL and capacity 0
+ * (counts only, to size the output).  Returns the request's own status. */
+fdas_status fdas_server_wait(fdas_server *s, uint64_t request_id, int32_t timeout_ms, fdas_candidate *out,
+                             uint32_t capacity, uint32_t *n_total, uint32_t *n_dropped, double *latency_ms);
+/* [0] completed, [1] queued, [2] in flight, [3] slots, [4] slot device bytes,
+ * [5] most requests in flight at once */
+fdas_status fdas_server_stats(fdas_server *s, uint64_t *out, uint32_t n);
+/* Message of the last failed request collected by fdas_server_wait. */
+const char *fdas_server_last_error(fdas_server *s);
+/* Stops the dispatcher (requests still queued are dropped) and frees the slots. */
+void fdas_server_destroy(fdas_server *s);
+
+/* ------------------------------------------------------------------------
+ * Batched search (no counterpart in the reference; the batched form).  Many
+ * trials (dedispersed spectra) of uneven length searched in one pass: one
+ * tiling launch and one persistent FT-convolution launch over the (trial,
+ * tile, template) items of all trials, then harmonic summing, FP64 recheck
+ * and candidate selection per trial on parallel branch streams; the sequence
+ * is captured once into a CUDA graph and replayed.  Before the capture an
+ * autotuner (cfg->autotune) times the FT convolution's FFT split (one warp,
+ * 64 x 32, or a warp pair, 32 x 64), its CTAs per SM and the harmonic-summing
+ * pipeline depth on the batch itself and keeps the fastest.  Every trial gets
+ * the candidates a plain search of it would give.
+ * ---------------------------------------------------------------------- */
+typedef struct fdas_batch fdas_batch;
+typedef struct {
+  int32_t device;
+  uint32_t n_planes;                    /* 1..16 */
+  uint32_t candidate_capacity;          /* hit records per trial (2^18) */
+  uint32_t candidates_per_plane_compat; /* fixed-size list entries per plane (512) */
+  uint32_t autotune;                    /* 1 = tune before the first capture */
+  uint32_t recheck;                     /* 1 = FP64 recheck of near-threshold cells */
+} fdas_batch_config;
+
+void fdas_batch_default_config(fdas_batch_config *cfg);
+/* Allocates for n_trials trials of n_bins[i] bins; the bank as for
+ * fdas_upload_templates (bank_len taps per row for the time-domain layout). */
+fdas_status fdas_batch_create(const fdas_batch_config *cfg, const fdas_complex *bank, fdas_template_layout layout,
+                              uint32_t bank_rows, uint32_t bank_len, uint32_t n_trials, const uint32_t *n_bins,
+                              fdas_batch **out);
+/* The trials' spectra, concatenated (sum of n_bins values), from host or
+ * device memory; enqueued before the next run. */
+fdas_status fdas_batch_set_inputs(fdas_batch *b, const fdas_complex *spectra, int on_device);
+/* Device address of the concatenated input spectra (for producers on the GPU). */
+fdas_complex *fdas_batch_input(fdas_batch *b);
+/* Search every trial with the n_planes thresholds (captures the graph on the
+ * first call and when the thresholds change; autotunes before the first
+ * capture).  wait != 0 blocks until done. */
+fdas_status fdas_batch_run(fdas_batch *b, const float *thresholds, int wait);
+fdas_status fdas_batch_wait(fdas_batch *b);
+/* A handle viewing trial `trial` after a run: use it with
+ * fdas_retrieve_candidate_list, fdas_retrieve_candidates, fdas_retrieve_fop
+ * and fdas_get_counters (buffer set A).  Owned by the batch. */
+fdas_handle *fdas_batch_trial(fdas_batch *b, uint32_t trial);
+/* out: [0] FFT split (1 one warp, 2 warp pair), [1] FT-convolution CTAs per SM,
+ * [2] lean harmonic summing, [3] tuned, [4] tiles of the batch, [5] configs
+ * timed; tune_ms: the autotuner's time per configuration. */
+fdas_status fdas_batch_info(fdas_batch *b, int32_t *out, uint32_t n, float *tune_ms, uint32_t n_ms);
+/* Fix the tuning by hand (skips the autotuner; the graph is recaptured). */
+fdas_status fdas_batch_set_tuning(fdas_batch *b, int32_t ftc_variant, int32_t ftc_ctas_per_sm, int32_t hsum_lean);
+const char *fdas_batch_last_error(const fdas_batch *b);
+void fdas_batch_destroy(fdas_batch *b);
 
 /* Library version string. */
 const char *fdas_version(void);
