@@ -13,6 +13,7 @@ constexpr int kWarpsPerCta = 8;
 // One warp per tile.  Tile i covers spectrum bins [i P - O, i P + P): bins
 // below 0 (the first tile's overlap) and from N on (the last tile's padding)
 // read as zero -- tile_input.cl.mako:42-94 / ft_conv.py:165-180.
+template <bool BATCH>
 __global__ void __launch_bounds__(256) tile_fft_kernel(TileParams p) {
   extern __shared__ float4 smem_f4[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -24,7 +25,7 @@ __global__ void __launch_bounds__(256) tile_fft_kernel(TileParams p) {
   const float2 *input = p.input;
   int n_bins = p.n_bins;
   long long local = tile;
-  if (p.trials) {  // batched: the trial's own spectrum and tile numbering
+  if constexpr (BATCH) {  // batched: the trial's own spectrum and tile numbering
     const BatchTrial &tr = p.trials[batch_trial_of(p.trials, p.n_trials, tile)];
     input += tr.input_offset;
     n_bins = tr.n_bins;
@@ -99,8 +100,9 @@ struct FopTarget {
   long long base;
   int n_bins;
 };
+template <bool BATCH>
 __device__ __forceinline__ FopTarget fop_target(const FtcParams &p, int tile, int row) {
-  if (!p.trials)
+  if constexpr (!BATCH)
     return FopTarget{p.fop + (long long)row * p.fop_stride, (long long)tile * p.payload - p.overlap, p.n_bins};
   const BatchTrial &tr = p.trials[batch_trial_of(p.trials, p.n_trials, tile)];
   return FopTarget{p.fop + tr.fop_offset + (long long)row * tr.stride,
@@ -118,6 +120,8 @@ __device__ __forceinline__ FopTarget fop_target(const FtcParams &p, int tile, in
 // 2048^2, utils.cl.mako:41-47); y = IFFT(Y);
 // FOP[row][i P + n - O] = |y[n]|^2 for n >= O, trimmed to N bins
 // (square_and_discard.cl.mako:28-76).
+// BATCH: tiles of several trials (trial table), else one spectrum's tiles
+template <bool BATCH>
 __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
   extern __shared__ float4 smem_f4[];
   __shared__ uint64_t bars[kWarpsPerCta];
@@ -161,7 +165,7 @@ __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
       if (next < n_items && lane == 0)
         prefetch_template(ex, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
     });
-    const FopTarget tg = fop_target(p, tile, row);
+    const FopTarget tg = fop_target<BATCH>(p, tile, row);
     sfor<2>([&](auto C) {
       constexpr int c = decltype(C)::value;
       sfor<32>([&](auto D) {
@@ -200,6 +204,7 @@ __device__ __forceinline__ bool pair_and(int pair, bool v) {
   return r != 0;
 }
 
+template <bool BATCH>
 __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
   extern __shared__ float4 smem_f4[];
   __shared__ uint64_t bars[kPairsPerCta];
@@ -254,7 +259,7 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
       if (next < n_items && tp == 0)
         prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
     });
-    const FopTarget tg = fop_target(p, tile, row);
+    const FopTarget tg = fop_target<BATCH>(p, tile, row);
     sfor<4>([&](auto R) {
       constexpr int r = decltype(R)::value;
       sfor<8>([&](auto D2) {
@@ -306,15 +311,12 @@ __global__ void taps_kernel(TapsParams p) {
 static int ex_smem_bytes() { return kWarpsPerCta * kExFloats * (int)sizeof(float); }
 
 cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s) {
-  static bool attr = false;
   const int smem = ex_smem_bytes();
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tile_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  auto kern = p.trials ? tile_fft_kernel<true> : tile_fft_kernel<false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
   dim3 grid((p.n_tiles + kWarpsPerCta - 1) / kWarpsPerCta);
-  tile_fft_kernel<<<grid, 256, smem, s>>>(p);
+  kern<<<grid, 256, smem, s>>>(p);
   return cudaGetLastError();
 }
 
@@ -341,17 +343,19 @@ cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
   const long long items = (long long)p.n_tiles * p.n_rows;
   if ((p.variant ? p.variant : ftc_variant()) == 1) {
     const int smem = ex_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(ftc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    auto kern = p.trials ? ftc_kernel<true> : ftc_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     const long long ctas = (items + kWarpsPerCta - 1) / kWarpsPerCta;
-    ftc_kernel<<<(int)(ctas < n_sm ? ctas : n_sm), 256, smem, s>>>(p);
+    kern<<<(int)(ctas < n_sm ? ctas : n_sm), 256, smem, s>>>(p);
   } else {
     const int smem = (kPairsPerCta * kEx2Floats + kTw2Floats) * (int)sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(ftc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    auto kern = p.trials ? ftc2_kernel<true> : ftc2_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     const long long ctas = (items + kPairsPerCta - 1) / kPairsPerCta;
     const long long per_sm = p.ctas_per_sm >= 1 && p.ctas_per_sm <= 2 ? p.ctas_per_sm : 2;
-    ftc2_kernel<<<(int)(ctas < per_sm * n_sm ? ctas : per_sm * n_sm), 256, smem, s>>>(p);
+    kern<<<(int)(ctas < per_sm * n_sm ? ctas : per_sm * n_sm), 256, smem, s>>>(p);
   }
   return cudaGetLastError();
 }
