@@ -178,7 +178,7 @@ __device__ __forceinline__ void add_rows(float (&acc)[4][8], const float (&c0)[8
 // accumulators in registers and stays small.  Each lane builds its hit mask,
 // a warp prefix sum gives every lane its slots in the warp's record buffer.
 struct Tile32 {
-  float v[32];  // v[8 k + e]: template |t| = t0 + k, bin F + e
+  float v[32];  // v[8 k + e]: template |t| = t0 + k, bin F + (e & 3) + 128 (e >> 2)
 };
 
 __device__ __noinline__ void emit_tile(EmitBuf &eb, const HsumParams &p, Tile32 tile,
@@ -209,7 +209,8 @@ __device__ __noinline__ void emit_tile(EmitBuf &eb, const HsumParams &p, Tile32 
       const int c = __ffs(nmask) - 1;
       nmask &= nmask - 1;
       if (base < (unsigned)p.rc_cap)
-        p.rc_list[base] = make_uint4((unsigned)plane, (unsigned)(H + sgn * (t0 + (c >> 3))), (unsigned)(F + (c & 7)), 0u);
+        p.rc_list[base] = make_uint4((unsigned)plane, (unsigned)(H + sgn * (t0 + (c >> 3))),
+                                     (unsigned)(F + (c & 3) + (((c >> 2) & 1) << 7)), 0u);
       else
         atomicOr(p.status, kStatusRecheckOverflow);
       ++base;
@@ -234,7 +235,7 @@ __device__ __noinline__ void emit_tile(EmitBuf &eb, const HsumParams &p, Tile32 
       const int c = __ffs(hmask) - 1;
       hmask &= hmask - 1;
       if (g < (unsigned)p.cand_cap) {
-        p.cand_key[g] = cand_key(plane, H + sgn * (t0 + (c >> 3)), F + (c & 7));
+        p.cand_key[g] = cand_key(plane, H + sgn * (t0 + (c >> 3)), F + (c & 3) + (((c >> 2) & 1) << 7));
         p.cand_pwr[g] = tile.v[c];
       }
       ++g;
@@ -324,7 +325,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
       const HsItem item = hs_item(p, it);
       const int f0 = item.f0, sgn = item.sgn;
       const float *stage = stages + st * p.stage_floats;
-      const int Fl = 8 * lane;  // first bin of the tile within the block
+      // lane l holds bins f0 + 4 l + {0..3} and f0 + 128 + 4 l + {0..3}: the
+      // lanes of a warp read consecutive 16-byte words (no bank conflicts)
+      const int Fl = 4 * lane;
       const int F = f0 + Fl;
       bool rowok[4];
 #pragma unroll
@@ -337,7 +340,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
         for (int kk = 0; kk < 4; ++kk) {
           const float *rr = r1 + srow(t0 + kk, kRows1, sgn) * kHsBins;
           const float4 q0 = *reinterpret_cast<const float4 *>(rr);
-          const float4 q1 = *reinterpret_cast<const float4 *>(rr + 4);
+          const float4 q1 = *reinterpret_cast<const float4 *>(rr + 128);
           acc[kk][0] = q0.x; acc[kk][1] = q0.y; acc[kk][2] = q0.z; acc[kk][3] = q0.w;
           acc[kk][4] = q1.x; acc[kk][5] = q1.y; acc[kk][6] = q1.z; acc[kk][7] = q1.w;
           if (!rowok[kk]) {
@@ -350,7 +353,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
             for (int e = 0; e < 8; ++e)
-              if (F + e >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
+              if (F + (e & 3) + ((e >> 2) << 7) >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
         }
       };
       load_plane1();
@@ -370,28 +373,32 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           const int a0 = (f0 / j) & ~3;
           const int bw = p.bw[j], bh = p.bh[j];
           const float *box = stage + p.soff[j];
+          // f0 is a multiple of 256, so for j = 2, 4, 8 the box starts at f0 / j
           if constexpr (j == 2) {
-            const float *r0 = box + srow(t0 / 2, bh, sgn) * bw + (F / 2 - a0);
-            const float4 v0 = *reinterpret_cast<const float4 *>(r0);
-            const float4 v1 = *reinterpret_cast<const float4 *>(r0 + sgn * bw);
+            const float *r0 = box + srow(t0 / 2, bh, sgn) * bw + 2 * lane;
+            const float *r1 = r0 + sgn * bw;
+            const float2 a0v = *reinterpret_cast<const float2 *>(r0), b0v = *reinterpret_cast<const float2 *>(r0 + 64);
+            const float2 a1v = *reinterpret_cast<const float2 *>(r1), b1v = *reinterpret_cast<const float2 *>(r1 + 64);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
-              const float4 v = kk < 2 ? v0 : v1;
-              acc[kk][0] += v.x; acc[kk][1] += v.x; acc[kk][2] += v.y; acc[kk][3] += v.y;
-              acc[kk][4] += v.z; acc[kk][5] += v.z; acc[kk][6] += v.w; acc[kk][7] += v.w;
+              const float2 va = kk < 2 ? a0v : a1v, vb = kk < 2 ? b0v : b1v;
+              acc[kk][0] += va.x; acc[kk][1] += va.x; acc[kk][2] += va.y; acc[kk][3] += va.y;
+              acc[kk][4] += vb.x; acc[kk][5] += vb.x; acc[kk][6] += vb.y; acc[kk][7] += vb.y;
             }
           } else if constexpr (j == 4) {
-            const float2 v = *reinterpret_cast<const float2 *>(box + srow(t0 / 4, bh, sgn) * bw + (F / 4 - a0));
+            const float *r0 = box + srow(t0 / 4, bh, sgn) * bw + lane;
+            const float va = r0[0], vb = r0[32];
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-              for (int e = 0; e < 8; ++e) acc[kk][e] += e < 4 ? v.x : v.y;
+              for (int e = 0; e < 8; ++e) acc[kk][e] += e < 4 ? va : vb;
           } else if constexpr (j == 8) {
-            const float v = box[srow(t0 / 8, bh, sgn) * bw + (F / 8 - a0)];
+            const float *r0 = box + srow(t0 / 8, bh, sgn) * bw + (lane >> 1);
+            const float va = r0[0], vb = r0[16];
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-              for (int e = 0; e < 8; ++e) acc[kk][e] += v;
+              for (int e = 0; e < 8; ++e) acc[kk][e] += e < 4 ? va : vb;
           } else {
             const int rb = t0 / j;
             const int kstar = j - (t0 - rb * j);  // warp-uniform: first k with trunc((t0+k)/j) = rb + 1
@@ -400,9 +407,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
             float c0[8], c1[8];
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-              const int o = (F + e) / j;
+              const int o = (F + (e & 3) + ((e >> 2) << 7)) / j;
               c0[e] = r0[o];
-              c1[e] = r1[o];
+              c1[e] = kstar < 4 ? r1[o] : 0.f;  // the second row only where the four rows split
             }
             switch (kstar < 4 ? kstar : 4) {
               case 1: add_rows<1>(acc, c0, c1); break;
