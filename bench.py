@@ -558,6 +558,54 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ precision form
+def run_precision(args):
+    """The 2^21-bin search with the inverse DFT of the FT convolution on the
+    tensor cores (split BF16 / split FP16 operands, tcgen05) beside the FP32 FFT
+    path: searches/s, FT-convolution stage time and whether the candidate set
+    equals the FP32 path's (errors against FP64 are measured by the tests)."""
+    import torch
+    from fdas_gb300.fdas import FDAS
+    torch.cuda.set_device(0)
+    x, bank, thr = make_inputs(args.bins, args.noise_only)
+    d_x = torch.from_numpy(x.view(np.float32)).cuda()
+    log = open(os.devnull, "w")
+    out = {}
+    ref_keys = None
+    for prec, name in ((0, "fp32_fft"), (1, "split_bf16_tcgen05"), (2, "split_fp16_tcgen05")):
+        h = FDAS(log)
+        assert h.initialise_accelerator(args.bins, precision=prec), h.last_error
+        assert h.upload_templates(bank, FDAS.A), h.last_error
+        for _ in range(args.warmup):
+            assert h.enqueue_search_device(d_x.data_ptr(), thr, FDAS.AllAccelerations, FDAS.A), h.last_error
+        assert h.synchronize(FDAS.A)
+        s = torch.cuda.ExternalStream(h.stream(FDAS.A))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(args.steps):
+            h.enqueue_search_device(d_x.data_ptr(), thr, FDAS.AllAccelerations, FDAS.A)
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        stages = []
+        for _ in range(5):
+            h.enqueue_search_device(d_x.data_ptr(), thr, FDAS.AllAccelerations, FDAS.A)
+            h.synchronize(FDAS.A)
+            stages.append(h.stage_times(FDAS.A))
+        st = np.mean(np.array(stages), axis=0)
+        rec, n_total, dropped = h.retrieve_candidate_list(FDAS.A)
+        keys = set(zip(rec["harmonic"].tolist(), rec["template_num"].tolist(), rec["bin"].tolist()))
+        if ref_keys is None:
+            ref_keys = keys
+        out[name] = {"searches_per_s": 1e3 / ms, "ms_per_search": ms, "ft_convolution_ms": float(st[2]),
+                     "candidates": n_total, "same_candidates_as_fp32": keys == ref_keys}
+        h.close()
+    line = {"form": "precision", "metric": "searches/s at 2^21 bins x 85 tmpl x 8 harm by inverse-DFT precision",
+            "unit": "searches/s", "n_bins": args.bins, "steps": args.steps, "warmup": args.warmup,
+            "results": out, "data": "synthetic", "timing": "CUDA events on the library stream, sequential searches"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -573,7 +621,7 @@ def main():
                     help="spectrum bins; the reported workload is 2^21, smaller values are for ncu captures")
     ap.add_argument("--trials", type=int, default=256, help="batched form: number of trials")
     ap.add_argument("--no-autotune", action="store_true", help="batched form: default tuning")
-    ap.add_argument("--form", default="plain", choices=["plain", "served", "batched"],
+    ap.add_argument("--form", default="plain", choices=["plain", "served", "batched", "precision"],
                     help="served: the request server under Poisson arrivals (prints its own JSON line)")
     ap.add_argument("--rate", type=float, default=200.0, help="served form: arrival rate (searches/s)")
     ap.add_argument("--requests", type=int, default=400, help="served form: number of requests")
@@ -586,6 +634,9 @@ def main():
         return
     if args.form == "batched":
         run_batched(args)
+        return
+    if args.form == "precision":
+        run_precision(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -36,6 +36,7 @@ class FdasConfig(ctypes.Structure):
         ("recheck", ctypes.c_uint32),
         ("recheck_band", ctypes.c_float),
         ("overlap", ctypes.c_uint32),
+        ("precision", ctypes.c_uint32),
     ]
 
 

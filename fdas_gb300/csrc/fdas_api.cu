@@ -286,6 +286,7 @@ fdas_status enqueue_ftc(fdas_handle *h, int ab, fdas_fop_part which) {
   p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlStatus);
   p.timeout_ns = 2000000000LL;  // 2 s
   p.ctas_per_sm = h->cfg.overlap ? 1 : 2;
+  p.variant = h->cfg.precision == 1 ? 3 : h->cfg.precision == 2 ? 4 : 0;
   CK(h, launch_ftc(p, S.stream));
   CK(h, cudaEventRecord(S.ev[3], S.stream));
   S.ev_ftc_recorded = true;
@@ -499,6 +500,7 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
   uint32_t pc = cfg.candidates_per_plane_compat ? cfg.candidates_per_plane_compat : 512u;
   if (pc > (uint32_t)kMaxCompat)
     return fail(nullptr, FDAS_ERR_INVALID_ARG, "candidates_per_plane_compat must be <= 2048");
+  if (cfg.precision > 2) return fail(nullptr, FDAS_ERR_INVALID_ARG, "precision must be 0, 1 or 2");
 
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);

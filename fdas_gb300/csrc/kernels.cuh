@@ -80,7 +80,8 @@ struct FtcParams {
   int *status;
   long long timeout_ns;
   int ctas_per_sm;        // persistent CTAs per SM (1 leaves room for harmonic summing)
-  int variant = 0;        // FFT split: 0 default, 1 one warp per item (64 x 32), 2 a warp pair (32 x 64)
+  int variant = 0;        // FFT split: 0 default, 1 one warp per item (64 x 32), 2 a warp pair (32 x 64);
+                          // 3 / 4: tensor-core DFT factors with split BF16 / FP16 operands
   const BatchTrial *trials = nullptr;  // batched search: tiles of all trials, FOPs per trial
   int n_trials = 0;
 };
@@ -200,6 +201,8 @@ cudaError_t launch_series_spectrum(const SeriesParams &p, cudaStream_t s);
 
 cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s);
 cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s);
+// precision form: inverse DFT on tcgen05 with split FP16 (f16) or BF16 operands
+cudaError_t launch_ftc_tc(const FtcParams &p, bool f16, cudaStream_t s);
 cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s);
 // consumer warps of the harmonic-summing kernel for `half` (4 templates each)
 int hsum_warps(int half);

@@ -340,6 +340,7 @@ cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
     if (n_sm <= 0) n_sm = 1;
   }
+  if ((p.variant == 3 || p.variant == 4) && !p.trials) return launch_ftc_tc(p, p.variant == 4, s);
   const long long items = (long long)p.n_tiles * p.n_rows;
   if ((p.variant ? p.variant : ftc_variant()) == 1) {
     const int smem = ex_smem_bytes();

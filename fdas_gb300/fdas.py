@@ -89,7 +89,8 @@ class FDAS:
     # -------------------------------------------------------- the class API
     def initialise_accelerator(self, input_sz, mode=PerSet, sync_pipeline=False, device=0, n_templates=85,
                                max_template_len=421, tile_overlap=0, n_planes=8, candidate_capacity=0,
-                               candidates_per_plane_compat=0, recheck=True, recheck_band=0.0, overlap=False):
+                               candidates_per_plane_compat=0, recheck=True, recheck_band=0.0, overlap=False,
+                               precision=0):
         """FDAS::initialise_accelerator (FDAS.h:44-49).  The bitstream and the
         OpenCL platform / device selectors become a CUDA device ordinal."""
         cfg = _lib.FdasConfig()
@@ -106,6 +107,7 @@ class FDAS:
         cfg.recheck = int(bool(recheck))
         cfg.recheck_band = float(recheck_band)
         cfg.overlap = int(bool(overlap))
+        cfg.precision = int(precision)
         if self._h:
             self._lib.fdas_destroy(self._h)
             self._h = ctypes.c_void_p()

@@ -98,6 +98,10 @@ typedef struct {
   uint32_t overlap;            /* 1 = size the kernels so that the FT convolution of one
                                   buffer set and the harmonic summing of the other run
                                   concurrently on every SM (for pipelined A/B searches) */
+  uint32_t precision;          /* inverse DFT of the FT convolution: 0 = FP32 FFT on the
+                                  CUDA cores (default); 1 / 2 = DFT-64 x DFT-32 factor
+                                  products on the tensor cores (tcgen05) with split
+                                  (hi + lo) BF16 / FP16 operands, FP32 accumulation */
 } fdas_config;
 
 /* Fill `cfg` with the reference's defaults for `n_frequency_bins` bins. */
