@@ -501,9 +501,18 @@ __global__ void __launch_bounds__(1024) select_hist_kernel(SelectParams p) {
   __syncthreads();
   const unsigned n = min(*p.cand_total, (unsigned)p.cand_cap);
   const unsigned K = (unsigned)p.per_plane;
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int plane = (int)(p.cand_key[i] >> 48);
-    if (p.cand_count[plane] > K) atomicAdd(sh_hist + plane * kSelBuckets + pwr_bucket(p.cand_pwr[i]), 1u);
+  // warp-uniform loop; lanes that hit the same (plane, bucket) -- common, since
+  // a signal's hits have similar powers -- add once, through their leader
+  const unsigned ln = threadIdx.x & 31;
+  for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += gridDim.x * blockDim.x) {
+    const unsigned i = base + ln;
+    unsigned slot = 0xffffffffu;
+    if (i < n) {
+      const int plane = (int)(p.cand_key[i] >> 48);
+      if (p.cand_count[plane] > K) slot = (unsigned)(plane * kSelBuckets + pwr_bucket(p.cand_pwr[i]));
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, slot);
+    if (slot != 0xffffffffu && ln == (unsigned)(__ffs(peers) - 1)) atomicAdd(sh_hist + slot, (unsigned)__popc(peers));
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nb; i += blockDim.x)

@@ -34,7 +34,9 @@ constexpr int kTcThreads = 256;
 // shared-memory regions (bytes); stage B's A operands (4 x 16 KB) reuse the
 // stage-A B operands once the stage-A products are done
 constexpr int kAAh = 0, kAAl = 32768, kBAh = 65536, kBAl = 98304, kBBh = 131072, kBBl = 139264;
-constexpr int kTcSmem = 147456;
+// + the inter-stage twiddles w^(n1 k2) at [k2][n1] (16 KB)
+constexpr int kTW = 147456;
+constexpr int kTcSmem = 163840;
 // tensor memory: stage A hi*hi at columns 0..127, its correction terms (hi*lo + lo*hi)
 // at 128..255; stage B hi*hi at 256 + 64 p, corrections at 384 + 64 p.  The small
 // corrections get their own FP32 accumulators and are added on the CUDA cores.
@@ -89,26 +91,23 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// hi / lo split of x in the operand type, as 16-bit patterns
-template <bool F16>
-__device__ __forceinline__ void split16(float x, unsigned short &hi, unsigned short &lo) {
-  if constexpr (F16) {
-    const __half h = __float2half_rn(x);
-    hi = __half_as_ushort(h);
-    lo = __half_as_ushort(__float2half_rn(x - __half2float(h)));
-  } else {
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
-    hi = __bfloat16_as_ushort(h);
-    lo = __bfloat16_as_ushort(__float2bfloat16_rn(x - __bfloat162float(h)));
-  }
-}
+// hi / lo split of two values at once (paired conversions), stored as two
+// 32-bit words: element pair (x0, x1) of the hi and of the lo operand
 template <bool F16>
 __device__ __forceinline__ void store_pair(uint8_t *hi_base, uint8_t *lo_base, int off, float x0, float x1) {
-  unsigned short h0, l0, h1, l1;
-  split16<F16>(x0, h0, l0);
-  split16<F16>(x1, h1, l1);
-  *reinterpret_cast<uint32_t *>(hi_base + off) = (uint32_t)h0 | ((uint32_t)h1 << 16);
-  *reinterpret_cast<uint32_t *>(lo_base + off) = (uint32_t)l0 | ((uint32_t)l1 << 16);
+  if constexpr (F16) {
+    const __half2 h = __floats2half2_rn(x0, x1);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(x0 - hf.x, x1 - hf.y);
+    *reinterpret_cast<__half2 *>(hi_base + off) = h;
+    *reinterpret_cast<__half2 *>(lo_base + off) = l;
+  } else {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+    *reinterpret_cast<__nv_bfloat162 *>(hi_base + off) = h;
+    *reinterpret_cast<__nv_bfloat162 *>(lo_base + off) = l;
+  }
 }
 
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }  // -126 <= e <= 127
@@ -164,6 +163,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
     }
     store_pair<F16>(BBh, BBl, kmaj(r, kp, 64), v[0], v[1]);
   }
+  float2 *TW = reinterpret_cast<float2 *>(tsm + kTW);
+  for (int i = tid; i < 64 * 32; i += kTcThreads) TW[i] = __ldg(p.twiddle + (i & 63) * (i >> 6));
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&bar)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -186,19 +187,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
   uint32_t phase = 0;
 
   for (int g = blockIdx.x; g < n_groups; g += gridDim.x) {
-    // ---- stage-A B operand: Y = tile spectrum x template spectrum, 4 items
-    // thread: k2 = lane, pairs (k1, k1 + 1) for 16 (item, k1-pair) slots
+    // ---- stage-A B operand: Y = tile spectrum x template spectrum, 4 items.
+    // A warp fills whole 8 x 8 core matrices per store (no bank conflicts):
+    // task t = (item, row group rg, K group kc); lane l: k2 = 8 rg + l / 4,
+    // k1 = 8 kc + 2 (l % 4) and k1 + 1
     float4 y[16];
     float mx = 0.f;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const int idx = warp + 8 * j, item = idx >> 5, k1 = (idx & 31) * 2;
+      const int t = warp + 8 * j, item = t >> 5, rg = (t >> 3) & 3, kc = t & 7;
+      const int k2 = 8 * rg + (lane >> 2), k1 = 8 * kc + 2 * (lane & 3);
       const int it = g * kTcItems + item;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       if (it < n_items) {
         const int tile = it / p.n_rows, row = p.row_begin + (it - tile * p.n_rows);
         const float2 *S = p.tiles + (long long)tile * kTile, *T = p.tmpl + (long long)row * kTile;
-        const int k = 32 * k1 + lane;
+        const int k = 32 * k1 + k2;
         const float2 s0 = __ldg(S + k), t0 = __ldg(T + k), s1 = __ldg(S + k + 32), t1 = __ldg(T + k + 32);
         v = make_float4(s0.x * t0.x - s0.y * t0.y, s0.x * t0.y + s0.y * t0.x, s1.x * t1.x - s1.y * t1.y,
                         s1.x * t1.y + s1.y * t1.x);
@@ -219,8 +223,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
     const float sa = pow2f(sigma);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const int idx = warp + 8 * j, item = idx >> 5, k1 = (idx & 31) * 2;
-      const int r = item * 32 + lane;
+      const int t = warp + 8 * j, item = t >> 5, rg = (t >> 3) & 3, kc = t & 7;
+      const int k1 = 8 * kc + 2 * (lane & 3);
+      const int r = item * 32 + 8 * rg + (lane >> 2);
       store_pair<F16>(BAh, BAl, kmaj(r, k1, 128), y[j].x * sa, y[j].z * sa);       // Re, k1 and k1 + 1
       store_pair<F16>(BAh, BAl, kmaj(r, 64 + k1, 128), y[j].y * sa, y[j].w * sa);  // Im
     }
@@ -265,7 +270,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
         for (int jj = 0; jj < 16; ++jj) {
           const float other = __shfl_xor_sync(0xffffffffu, v[jj], 1);
           const float zr = part ? other : v[jj], zi = part ? v[jj] : other;
-          const float2 w = __ldg(p.twiddle + n1 * (kb + jj));
+          const float2 w = TW[(kb + jj) * 64 + n1];
           z[jj] = (part == 0 ? zr * w.x - zi * w.y : zr * w.y + zi * w.x) * (1.0f / 64.0f);
         }
         uint8_t *abh = tsm + kBAh + h * 32768, *abl = abh + 16384;
