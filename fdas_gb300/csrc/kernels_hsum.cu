@@ -524,13 +524,17 @@ __global__ void __launch_bounds__(1024) select_hist_kernel(SelectParams p) {
   __syncthreads();
   if (!last) return;
   __threadfence();
+  // the summed histograms into shared memory (one coalesced pass), so the
+  // boundary search below is not a chain of dependent global loads
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sh_hist[i] = __ldcg(p.hist + i);
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp < p.n_planes) {
     const int plane = warp;
     if (p.cand_count[plane] <= K) {
       if (lane == 0) p.sel_bucket[plane] = -1;
     } else {
-      volatile unsigned *h = p.hist + plane * kSelBuckets;
+      const unsigned *h = sh_hist + plane * kSelBuckets;
       // strongest first: chunk c covers buckets [2048 - 32 (c+1), 2048 - 32 c)
       unsigned above = 0;
       int found = -1;

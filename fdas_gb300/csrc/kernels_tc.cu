@@ -79,16 +79,17 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, 
       "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+// 32 consecutive tensor-memory columns of this thread's lane, one round trip
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float *v) {
+  uint32_t r[32];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
 #pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 // hi / lo split of two values at once (paired conversions), stored as two
@@ -197,16 +198,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
     for (int j = 0; j < 16; ++j) {
       const int t = warp + 8 * j, item = t >> 5, rg = (t >> 3) & 3, kc = t & 7;
       const int k2 = 8 * rg + (lane >> 2), k1 = 8 * kc + 2 * (lane & 3);
-      const int it = g * kTcItems + item;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (it < n_items) {
-        const int tile = it / p.n_rows, row = p.row_begin + (it - tile * p.n_rows);
-        const float2 *S = p.tiles + (long long)tile * kTile, *T = p.tmpl + (long long)row * kTile;
-        const int k = 32 * k1 + k2;
-        const float2 s0 = __ldg(S + k), t0 = __ldg(T + k), s1 = __ldg(S + k + 32), t1 = __ldg(T + k + 32);
-        v = make_float4(s0.x * t0.x - s0.y * t0.y, s0.x * t0.y + s0.y * t0.x, s1.x * t1.x - s1.y * t1.y,
-                        s1.x * t1.y + s1.y * t1.x);
-      }
+      // loads are unconditional (a missing item reads item 0 and is zeroed), so
+      // all 64 of a thread's loads are in flight together
+      const int it = g * kTcItems + item, itc = it < n_items ? it : 0;
+      const int tile = itc / p.n_rows, row = p.row_begin + (itc - tile * p.n_rows);
+      const float2 *S = p.tiles + (long long)tile * kTile, *T = p.tmpl + (long long)row * kTile;
+      const int k = 32 * k1 + k2;
+      const float2 s0 = __ldg(S + k), t0 = __ldg(T + k), s1 = __ldg(S + k + 32), t1 = __ldg(T + k + 32);
+      float4 v = make_float4(s0.x * t0.x - s0.y * t0.y, s0.x * t0.y + s0.y * t0.x, s1.x * t1.x - s1.y * t1.y,
+                             s1.x * t1.y + s1.y * t1.x);
+      if (it >= n_items) v = make_float4(0.f, 0.f, 0.f, 0.f);
       y[j] = v;
       mx = fmaxf(mx, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
     }
@@ -258,16 +259,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
     {
       const int m = 32 * q + lane, n1 = m >> 1, part = m & 1;
 #pragma unroll 1
-      for (int c = 0; c < 4; ++c) {
-        const int item = 2 * h + (c >> 1), kb = 16 * (c & 1);
-        float v[16], vc[16];
-        tc_ld16(tmem + lane_addr + (uint32_t)(64 * h + 16 * c), v);
-        tc_ld16(tmem + lane_addr + (uint32_t)(128 + 64 * h + 16 * c), vc);
+      for (int c = 0; c < 2; ++c) {
+        const int item = 2 * h + c, kb = 0;
+        float v[32], vc[32];
+        tc_ld32(tmem + lane_addr + (uint32_t)(64 * h + 32 * c), v);
+        tc_ld32(tmem + lane_addr + (uint32_t)(128 + 64 * h + 32 * c), vc);
 #pragma unroll
-        for (int jj = 0; jj < 16; ++jj) v[jj] += vc[jj];
-        float z[16];
+        for (int jj = 0; jj < 32; ++jj) v[jj] += vc[jj];
+        float z[32];
 #pragma unroll
-        for (int jj = 0; jj < 16; ++jj) {
+        for (int jj = 0; jj < 32; ++jj) {
           const float other = __shfl_xor_sync(0xffffffffu, v[jj], 1);
           const float zr = part ? other : v[jj], zi = part ? v[jj] : other;
           const float2 w = TW[(kb + jj) * 64 + n1];
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
         uint8_t *abh = tsm + kBAh + h * 32768, *abl = abh + 16384;
         const int r = (item & 1) * 64 + n1;
 #pragma unroll
-        for (int jj = 0; jj < 16; jj += 2) store_pair<F16>(abh, abl, kmaj(r, part * 32 + kb + jj, 64), z[jj], z[jj + 1]);
+        for (int jj = 0; jj < 32; jj += 2) store_pair<F16>(abh, abl, kmaj(r, part * 32 + kb + jj, 64), z[jj], z[jj + 1]);
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -314,12 +315,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
       const int it = g * kTcItems + 2 * h + iip;
       float y[64];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        float cm[16];
-        tc_ld16(tmem + lane_addr + (uint32_t)(256 + 64 * h + 16 * c), *reinterpret_cast<float(*)[16]>(y + 16 * c));
-        tc_ld16(tmem + lane_addr + (uint32_t)(384 + 64 * h + 16 * c), cm);
+      for (int c = 0; c < 2; ++c) {
+        float cm[32];
+        tc_ld32(tmem + lane_addr + (uint32_t)(256 + 64 * h + 32 * c), y + 32 * c);
+        tc_ld32(tmem + lane_addr + (uint32_t)(384 + 64 * h + 32 * c), cm);
 #pragma unroll
-        for (int jj = 0; jj < 16; ++jj) y[16 * c + jj] += cm[jj];
+        for (int jj = 0; jj < 32; ++jj) y[32 * c + jj] += cm[jj];
       }
       const float *yr = y, *yi = y + 32;
       if (it < n_items) {
