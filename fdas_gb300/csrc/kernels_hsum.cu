@@ -405,9 +405,14 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
             const float *r0 = box + srow(rb, bh, sgn) * bw - a0;
             const float *r1 = r0 + sgn * bw;
             float c0[8], c1[8];
+            // bins F + c and F + 128 + c (c < 4) sit at (F + c) / j = qa + (ra + c >= j)
+            // (ra + 3 < 2 j), and likewise for the second group: two divisions per plane
+            const int qa = F / j, ra = F - qa * j;
+            const int qb = (F + 128) / j, rg = F + 128 - qb * j;
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-              const int o = (F + (e & 3) + ((e >> 2) << 7)) / j;
+              const int c = e & 3;
+              const int o = e < 4 ? qa + (ra + c >= j ? 1 : 0) : qb + (rg + c >= j ? 1 : 0);
               c0[e] = r0[o];
               c1[e] = kstar < 4 ? r1[o] : 0.f;  // the second row only where the four rows split
             }
