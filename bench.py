@@ -56,7 +56,7 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -69,7 +69,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -118,11 +118,19 @@ def measured_peaks():
 
 
 # ------------------------------------------------------------------ CPU side
-def cpu_fop_rows(args):
+_WORKER = {}
+
+
+def cpu_worker_init(x, bank, dtype):
+    """Pool initializer: the spectrum and bank are sent to each worker once."""
+    _WORKER.update(x=x, bank=bank, dtype=dtype)
+
+
+def cpu_fop_rows(rows):
     """FOP rows by direct convolution (ft_conv.py:199-205 semantics)."""
     from oracle import fdas_oracle as O
-    x, bank, rows, dtype = args
-    return O.fop(x, bank, dtype=dtype, rows=rows)
+    O.fop(_WORKER["x"], _WORKER["bank"], dtype=_WORKER["dtype"], rows=rows)
+    return len(rows)
 
 
 def cpu_search_time(x, bank, thr, n_rows_sample, bin_frac, dtype, pool=None, workers=1):
@@ -138,7 +146,7 @@ def cpu_search_time(x, bank, thr, n_rows_sample, bin_frac, dtype, pool=None, wor
     t0 = time.perf_counter()
     if pool is not None:
         chunks = np.array_split(rows, workers)
-        pool.map(cpu_fop_rows, [(x, bank, list(c), dtype) for c in chunks if len(c)])
+        pool.map(cpu_fop_rows, [list(c) for c in chunks if len(c)])
     else:
         O.fop(x, bank, dtype=dtype, rows=rows)
     t_fop = (time.perf_counter() - t0) * N_TEMPLATES / n_rows_sample
@@ -177,7 +185,7 @@ def run_reference(args):
     import multiprocessing as mp
     # one row per worker and 1/64 of the bins per step keeps a step near half
     # a second on 16 cores, so --steps K --warmup W ends within minutes
-    with mp.get_context("spawn").Pool(workers) as pool:
+    with mp.get_context("spawn").Pool(workers, initializer=cpu_worker_init, initargs=(x, bank, np.float32)) as pool:
         for i in range(args.warmup + args.steps):
             t, desc = cpu_search_time(x, bank, thr, n_rows_sample=min(N_TEMPLATES, workers), bin_frac=1 / 64,
                                       dtype=np.float32, pool=pool, workers=workers)
@@ -609,7 +617,10 @@ def run_precision(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps; default 1500 searches for the GPU arm (a timed region above a "
+                         "second, so the clock sampler sees it several times), 5 for the reference arm "
+                         "and the batched form, 50 for the precision form")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--stage-times", action="store_true", help="per-step stage events inside the timed loop")
@@ -627,6 +638,9 @@ def main():
     ap.add_argument("--requests", type=int, default=400, help="served form: number of requests")
     ap.add_argument("--slots", type=int, default=8, help="served form: searches in flight at most")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if (args.impl == "reference" or args.form == "batched") else \
+            50 if args.form == "precision" else 1500
     if args.warmup < 3:
         args.warmup = 3
     if args.form == "served":

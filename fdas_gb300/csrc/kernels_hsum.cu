@@ -163,13 +163,27 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
 // boxes hold FOP rows in ascending order, i.e. reversed for the negative half
 __device__ __forceinline__ int srow(int r, int bh, int sgn) { return sgn > 0 ? r : bh - 1 - r; }
 
+// (a0, a1) += (b0, b1) as one packed FP32 pair instruction (add.rn.f32x2,
+// sm_100 and later): each half is an ordinary round-to-nearest FP32 add, so
+// the sums are the scalar ones bit for bit
+__device__ __forceinline__ void add2(float &a0, float &a1, float b0, float b1) {
+  unsigned long long a, b, d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(a0), "f"(a1));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(b) : "f"(b0), "f"(b1));
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a0), "=f"(a1) : "l"(d));
+}
+
 // acc[k][e] += (k < KS ? c0[e] : c1[e]), KS compile time
 template <int KS>
 __device__ __forceinline__ void add_rows(float (&acc)[4][8], const float (&c0)[8], const float (&c1)[8]) {
 #pragma unroll
   for (int k = 0; k < 4; ++k)
 #pragma unroll
-    for (int e = 0; e < 8; ++e) acc[k][e] += k < KS ? c0[e] : c1[e];
+    for (int e = 0; e < 8; e += 2) {
+      if (k < KS) add2(acc[k][e], acc[k][e + 1], c0[e], c0[e + 1]);
+      else add2(acc[k][e], acc[k][e + 1], c1[e], c1[e + 1]);
+    }
 }
 
 // Emission of plane `plane` (0-based) from the tile values; called by the
@@ -382,8 +396,10 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
               const float2 va = kk < 2 ? a0v : a1v, vb = kk < 2 ? b0v : b1v;
-              acc[kk][0] += va.x; acc[kk][1] += va.x; acc[kk][2] += va.y; acc[kk][3] += va.y;
-              acc[kk][4] += vb.x; acc[kk][5] += vb.x; acc[kk][6] += vb.y; acc[kk][7] += vb.y;
+              add2(acc[kk][0], acc[kk][1], va.x, va.x);
+              add2(acc[kk][2], acc[kk][3], va.y, va.y);
+              add2(acc[kk][4], acc[kk][5], vb.x, vb.x);
+              add2(acc[kk][6], acc[kk][7], vb.y, vb.y);
             }
           } else if constexpr (j == 4) {
             const float *r0 = box + srow(t0 / 4, bh, sgn) * bw + lane;
@@ -391,14 +407,14 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-              for (int e = 0; e < 8; ++e) acc[kk][e] += e < 4 ? va : vb;
+              for (int e = 0; e < 8; e += 2) add2(acc[kk][e], acc[kk][e + 1], e < 4 ? va : vb, e < 4 ? va : vb);
           } else if constexpr (j == 8) {
             const float *r0 = box + srow(t0 / 8, bh, sgn) * bw + (lane >> 1);
             const float va = r0[0], vb = r0[16];
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-              for (int e = 0; e < 8; ++e) acc[kk][e] += e < 4 ? va : vb;
+              for (int e = 0; e < 8; e += 2) add2(acc[kk][e], acc[kk][e + 1], e < 4 ? va : vb, e < 4 ? va : vb);
           } else {
             const int rb = t0 / j;
             const int kstar = j - (t0 - rb * j);  // warp-uniform: first k with trunc((t0+k)/j) = rb + 1
