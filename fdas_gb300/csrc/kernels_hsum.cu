@@ -380,7 +380,12 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
         emit_tile(eb, p, tile, plane, H, sgn, t0, F);
       };
       // rare: some lane of the warp reached the band of the plane (warp-uniform)
-      if (__any_sync(0xffffffffu, max32(acc) >= p.trig[0])) emit(0);
+      // ub: an upper bound of the lane's tile maximum.  Rounded addition is
+      // monotone, so ub + (largest value added) bounds every new sum, and the
+      // exact maximum (a 3-input max tree) is only needed where the bound reaches
+      // a plane's band
+      float ub = max32(acc);
+      if (__any_sync(0xffffffffu, ub >= p.trig[0])) emit(0);
       hs_sfor<MAXP - 1>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value + 2;
         if (j <= P) {
@@ -388,11 +393,13 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           const int bw = p.bw[j], bh = p.bh[j];
           const float *box = stage + p.soff[j];
           // f0 is a multiple of 256, so for j = 2, 4, 8 the box starts at f0 / j
+          float vmax;
           if constexpr (j == 2) {
             const float *r0 = box + srow(t0 / 2, bh, sgn) * bw + 2 * lane;
             const float *r1 = r0 + sgn * bw;
             const float2 a0v = *reinterpret_cast<const float2 *>(r0), b0v = *reinterpret_cast<const float2 *>(r0 + 64);
             const float2 a1v = *reinterpret_cast<const float2 *>(r1), b1v = *reinterpret_cast<const float2 *>(r1 + 64);
+            vmax = fmax3(fmax3(a0v.x, a0v.y, b0v.x), fmax3(b0v.y, a1v.x, a1v.y), fmaxf(b1v.x, b1v.y));
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
               const float2 va = kk < 2 ? a0v : a1v, vb = kk < 2 ? b0v : b1v;
@@ -404,6 +411,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           } else if constexpr (j == 4) {
             const float *r0 = box + srow(t0 / 4, bh, sgn) * bw + lane;
             const float va = r0[0], vb = r0[32];
+            vmax = fmaxf(va, vb);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
@@ -411,6 +419,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           } else if constexpr (j == 8) {
             const float *r0 = box + srow(t0 / 8, bh, sgn) * bw + (lane >> 1);
             const float va = r0[0], vb = r0[16];
+            vmax = fmaxf(va, vb);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
@@ -432,6 +441,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
               c0[e] = r0[o];
               c1[e] = kstar < 4 ? r1[o] : 0.f;  // the second row only where the four rows split
             }
+            vmax = fmax3(fmax3(c0[0], c0[1], c0[2]), fmax3(c0[3], c0[4], c0[5]), fmaxf(c0[6], c0[7]));
+            if (kstar < 4)
+              vmax = fmax3(vmax, fmax3(fmax3(c1[0], c1[1], c1[2]), fmax3(c1[3], c1[4], c1[5]), c1[6]), c1[7]);
             switch (kstar < 4 ? kstar : 4) {
               case 1: add_rows<1>(acc, c0, c1); break;
               case 2: add_rows<2>(acc, c0, c1); break;
@@ -439,7 +451,11 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
               default: add_rows<4>(acc, c0, c1); break;
             }
           }
-          if (__any_sync(0xffffffffu, max32(acc) >= p.trig[j - 1])) emit(j - 1);
+          ub += vmax;
+          if (__any_sync(0xffffffffu, ub >= p.trig[j - 1])) {
+            ub = max32(acc);
+            if (__any_sync(0xffffffffu, ub >= p.trig[j - 1])) emit(j - 1);
+          }
         }
       });
 
