@@ -89,37 +89,42 @@ struct EmitBuf {
 // Persistent harmonic summing.  Work item = (256-bin block, sign half),
 // handed out dynamically through a global counter.  A CTA has NW consumer
 // warps -- warp w owns templates |t| = 4w + k (k < 4), lane l the bins
-// f0 + 8 l + e (e < 8), i.e. a 4 x 8 tile of cells aligned to 4 and 8 -- and
-// one producer warp.  For every item the producer issues one 2-D TMA tensor
-// copy per plane (cp.async.bulk.tensor.2d): plane 1 as 256 bins x 4 NW rows,
-// plane j >= 2 as the rows trunc(t/j) of the half over bins [(f0/j) & ~3, ...);
-// rows and bins outside the FOP are zero-filled by the hardware (they only
-// feed masked cells).  kHsStages stages deep: full / empty mbarriers, every
-// wait bounded by %globaltimer.
+// f0 + 4 l + c and f0 + 128 + 4 l + c (c < 4), i.e. a 4 x 8 tile of cells --
+// and one producer warp.  For every item the producer issues one 2-D TMA
+// tensor copy per plane (cp.async.bulk.tensor.2d): plane 1 as 256 bins x 4 NW
+// rows, plane j >= 2 as the rows trunc(t/j) of the half over bins
+// [(f0/j) & ~3, ...); rows and bins outside the FOP are zero-filled by the
+// hardware (they only feed masked cells).  kHsStages stages deep: full / empty
+// mbarriers, every wait bounded by %globaltimer.
 //
-// With the tile aligned, planes 2, 4 and 8 read their values with 16-, 8- and
-// 4-byte loads at compile-time offsets; for planes 3, 5, 6, 7 the eight bins
-// map onto per-bin offsets computed once per item and the four rows onto two
-// staged rows split at a warp-uniform point, handled by a switch.
+// Planes 2, 4 and 8 read their values with 8- and 4-byte loads at
+// compile-time offsets; for planes 3, 5, 6, 7 the eight bins map onto offsets
+// from two divisions per plane and the four rows onto two staged rows split at
+// a warp-uniform point, handled by a switch.
 //
 // HP_1 = FOP[t][f], HP_j = HP_{j-1} + FOP[trunc(t/j)][f/j] accumulated in FP32
 // in this order -- hsum.py:95-120 / hms_baseline.cl.mako:55-84 -- so the
 // values match hsum.py bit for bit for the same FOP.  A cell is a candidate of
 // plane j if HP_j > thr_j (strict, hsum.py:134 / detect.cl.mako:185).  The fast
-// path only takes the maximum of the tile per plane; if some lane of the warp
-// reaches the lower edge of a plane's band, the warp recomputes its sums plane
-// by plane and emits through ballots.
+// path only tracks a bound of the tile maximum per plane and marks the planes
+// where some lane of the warp reaches the lower edge of the band; at the end
+// of the item, while the stage is still held, the warp recomputes its sums
+// plane by plane (same values, same order) and emits at the marked planes.
 struct HsItem {
   int f0, sgn, tlo;
 };
 
 __device__ __forceinline__ HsItem hs_item(const HsumParams &p, int it) {
-  // items enumerate (block, half) over the enabled halves
+  // items enumerate (block, half) over the enabled halves, highest blocks
+  // first: a signal's harmonic images cover wider bin ranges at higher bins
+  // (plane j sums f/k for k <= j), so the items that emit most are handed
+  // out early and the light ones fill the end of the launch
   const bool neg = p.tlo[0] <= p.half, pos = p.tlo[1] <= p.half;
+  const int nb = (p.n_bins + kHsBins - 1) / kHsBins;
   int blk, halfsel;
   if (neg && pos) { blk = it >> 1; halfsel = it & 1; }
   else { blk = it; halfsel = pos ? 1 : 0; }
-  return HsItem{blk * kHsBins, halfsel ? 1 : -1, p.tlo[halfsel]};
+  return HsItem{(nb - 1 - blk) * kHsBins, halfsel ? 1 : -1, p.tlo[halfsel]};
 }
 
 __device__ __forceinline__ int hs_n_items(const HsumParams &p) {
@@ -186,79 +191,155 @@ __device__ __forceinline__ void add_rows(float (&acc)[4][8], const float (&c0)[8
     }
 }
 
-// Emission of plane `plane` (0-based) from the tile values; called by the
-// whole warp when some lane's tile reached the lower edge of the plane's band.
-// Out of line, with the tile passed by value, so the hot loop keeps its
-// accumulators in registers and stays small.  Each lane builds its hit mask,
-// a warp prefix sum gives every lane its slots in the warp's record buffer.
-struct Tile32 {
-  float v[32];  // v[8 k + e]: template |t| = t0 + k, bin F + (e & 3) + 128 (e >> 2)
-};
+// Plane 1 of the warp's tile: 4 templates x 8 bins; cells outside the
+// item's rows or beyond n_bins are -inf (they never reach a threshold)
+template <int NW>
+__device__ __forceinline__ void hs_load_plane1(float (&acc)[4][8], const float *stage, const HsumParams &p,
+                                               int f0, int sgn, int tlo, int t0, int F) {
+  const int H = p.half;
+  const float *r1 = stage + p.soff[1] + (F - f0);
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk) {
+    const float *rr = r1 + srow(t0 + kk, 4 * NW, sgn) * kHsBins;
+    const float4 q0 = *reinterpret_cast<const float4 *>(rr);
+    const float4 q1 = *reinterpret_cast<const float4 *>(rr + 128);
+    acc[kk][0] = q0.x; acc[kk][1] = q0.y; acc[kk][2] = q0.z; acc[kk][3] = q0.w;
+    acc[kk][4] = q1.x; acc[kk][5] = q1.y; acc[kk][6] = q1.z; acc[kk][7] = q1.w;
+    if (!((t0 + kk <= H) && (t0 + kk >= tlo))) {
+#pragma unroll
+      for (int e = 0; e < 8; ++e) acc[kk][e] = -CUDART_INF_F;
+    }
+  }
+  if (f0 + kHsBins > p.n_bins) {
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        if (F + (e & 3) + ((e >> 2) << 7) >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
+  }
+}
 
-__device__ __noinline__ void emit_tile(EmitBuf &eb, const HsumParams &p, Tile32 tile,
-                                       int plane, int H, int sgn, int t0, int F) {
+// Plane j >= 2 added for any j given at run time: the same values in the same
+// order as the kernel's specialised per-plane code, so the sums are the same
+// bit for bit
+__device__ __forceinline__ void hs_add_plane_any(float (&acc)[4][8], const float *stage, const HsumParams &p,
+                                                 int j, int f0, int sgn, int t0, int F) {
+  const int a0 = (f0 / j) & ~3;
+  const int bw = p.bw[j];
+  const int rb = t0 / j;
+  const int kstar = j - (t0 - rb * j);  // first k with trunc((t0+k)/j) = rb + 1
+  const float *r0 = stage + p.soff[j] + srow(rb, p.bh[j], sgn) * bw - a0;
+  const float *r1 = r0 + sgn * bw;
+  // (F + c) / j = qa + [ra + c >= j] + [ra + c >= 2 j] for c < 4 <= 2 j
+  const int qa = F / j, ra = F - qa * j;
+  const int qb = (F + 128) / j, rg = F + 128 - qb * j;
+  float c0[8], c1[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    const int r = (e < 4 ? ra : rg) + (e & 3);
+    const int o = (e < 4 ? qa : qb) + (r >= j ? 1 : 0) + (r >= 2 * j ? 1 : 0);
+    c0[e] = r0[o];
+    c1[e] = kstar < 4 ? r1[o] : 0.f;
+  }
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+      const bool second = kk >= kstar;
+      add2(acc[kk][e], acc[kk][e + 1], second ? c1[e] : c0[e], second ? c1[e + 1] : c0[e + 1]);
+    }
+}
+
+// The lanes' cells of `mask` (bit c = cell 8 k + e: template |t| = t0 + k,
+// bin F + (e & 3) + 128 (e >> 2)) get consecutive slots from `pos`, cell by
+// cell, so every store instruction of the warp writes one contiguous run
+template <typename Put>
+__device__ __forceinline__ void hs_scatter(const float (&acc)[4][8], unsigned mask, unsigned pos, int row0, int sgn,
+                                           int F, Put &&put) {
+  const unsigned below = (1u << (threadIdx.x & 31)) - 1u;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    const unsigned m = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
+    if (m) {
+      if ((mask >> c) & 1u)
+        put(pos + __popc(m & below), acc[c >> 3][c & 7], row0 + sgn * (c >> 3), F + (c & 3) + (((c >> 2) & 1) << 7));
+      pos += __popc(m);
+    }
+  }
+}
+
+// Hits of plane `plane` (0-based) to the global list -- one reservation for
+// the warp -- and cells within the band to the FP64 recheck list
+__device__ __forceinline__ void hs_emit_plane(const float (&acc)[4][8], const HsumParams &p, EmitBuf *eb, int plane,
+                                              int row0, int sgn, int F) {
   const int lane = threadIdx.x & 31;
   const float hi = p.hi[plane], lo = p.lo[plane];
   unsigned hmask = 0, nmask = 0;
 #pragma unroll
   for (int c = 0; c < 32; ++c) {
-    const float a = tile.v[c];  // -inf for masked cells
+    const float a = acc[c >> 3][c & 7];
     if (a > hi) hmask |= 1u << c;
     else if (a >= lo) nmask |= 1u << c;
   }
-  // near-threshold cells go to the FP64 recheck list
-  unsigned nn = __popc(nmask);
-  unsigned ntot = nn;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned u = __shfl_up_sync(0xffffffffu, ntot, o);
-    if (lane >= o) ntot += u;
-  }
-  const unsigned nall = __shfl_sync(0xffffffffu, ntot, 31);
+  const unsigned nall = __reduce_add_sync(0xffffffffu, (unsigned)__popc(nmask));
   if (nall) {
     unsigned base = 0;
-    if (lane == 31) base = atomicAdd(p.rc_count, nall);
-    base = __shfl_sync(0xffffffffu, base, 31) + ntot - nn;
-    while (nmask) {
-      const int c = __ffs(nmask) - 1;
-      nmask &= nmask - 1;
-      if (base < (unsigned)p.rc_cap)
-        p.rc_list[base] = make_uint4((unsigned)plane, (unsigned)(H + sgn * (t0 + (c >> 3))),
-                                     (unsigned)(F + (c & 3) + (((c >> 2) & 1) << 7)), 0u);
-      else
-        atomicOr(p.status, kStatusRecheckOverflow);
-      ++base;
-    }
+    if (lane == 0) base = atomicAdd(p.rc_count, nall);
+    uint4 *list = p.rc_list;
+    const unsigned cap = (unsigned)p.rc_cap;
+    int *status = p.status;
+    hs_scatter(acc, nmask, __shfl_sync(0xffffffffu, base, 0), row0, sgn, F, [&](unsigned g, float, int row, int bin) {
+      if (g < cap) list[g] = make_uint4((unsigned)plane, (unsigned)row, (unsigned)bin, 0u);
+      else atomicOr(status, kStatusRecheckOverflow);
+    });
   }
-  // hits: one warp-aggregated reservation in the global list, then every lane
-  // stores its own records there directly (no staging, no further atomics)
-  const unsigned hn = __popc(hmask);
-  unsigned incl = hn;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += u;
-  }
-  const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+  const unsigned total = __reduce_add_sync(0xffffffffu, (unsigned)__popc(hmask));
   if (total) {
     unsigned base = 0;
-    if (lane == 31) base = atomicAdd(p.cand_total, total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    unsigned g = base + incl - hn;
-    while (hmask) {
-      const int c = __ffs(hmask) - 1;
-      hmask &= hmask - 1;
-      if (g < (unsigned)p.cand_cap) {
-        p.cand_key[g] = cand_key(plane, H + sgn * (t0 + (c >> 3)), F + (c & 3) + (((c >> 2) & 1) << 7));
-        p.cand_pwr[g] = tile.v[c];
+    if (lane == 0) base = atomicAdd(p.cand_total, total);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    unsigned long long *keys = p.cand_key;
+    float *pwrs = p.cand_pwr;
+    const unsigned cap = (unsigned)p.cand_cap;
+    hs_scatter(acc, hmask, base, row0, sgn, F, [&](unsigned g, float v, int row, int bin) {
+      if (g < cap) {
+        keys[g] = cand_key(plane, row, bin);
+        pwrs[g] = v;
       }
-      ++g;
-    }
+    });
     if (lane == 0) {
-      atomicAdd(&eb.pc[plane], total);
-      if (base + total > (unsigned)p.cand_cap) atomicOr(p.status, kStatusCandidateOverflow);
+      atomicAdd(&eb->pc[plane], total);
+      if (base + total > cap) atomicOr(p.status, kStatusCandidateOverflow);
     }
   }
+}
+
+// Emission for one item (rare; the warp calls it together, before it releases
+// the stage): the sums are recomputed plane by plane from the staged boxes
+// and the planes marked in `need` (bit j - 1) are emitted.
+template <int NW>
+__device__ __forceinline__ void hs_emit_item_body(const HsumParams &p, const float *stage, EmitBuf *eb, int f0,
+                                                  int sgn, int tlo, int t0, unsigned need) {
+  const int F = f0 + 4 * (threadIdx.x & 31);
+  const int row0 = p.half + sgn * t0;
+  float acc[4][8];
+  hs_load_plane1<NW>(acc, stage, p, f0, sgn, tlo, t0, F);
+#pragma unroll 1
+  for (int j = 1; j <= p.n_planes; ++j) {
+    if (j > 1) hs_add_plane_any(acc, stage, p, j, f0, sgn, t0, F);
+    if ((need >> (j - 1)) & 1u) hs_emit_plane(acc, p, eb, j - 1, row0, sgn, F);
+    if (!(need >> j)) break;
+  }
+}
+
+// The same out of line (the hot loop keeps its code and registers); `pp` is
+// the CTA's shared-memory copy of the parameters.  Used where registers are
+// plentiful: at the lean variant's 80 registers the call's saves would spill
+// in the hot loop, so that variant inlines the body.
+template <int NW>
+__device__ __noinline__ void hs_emit_item(const HsumParams *pp, const float *stage, EmitBuf *eb, int f0, int sgn,
+                                          int tlo, int t0, unsigned need) {
+  hs_emit_item_body<NW>(*pp, stage, eb, f0, sgn, tlo, t0, need);
 }
 
 template <int MAXP, int NW, int kHsStages, int MINB>
@@ -268,6 +349,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
   uint64_t *full = reinterpret_cast<uint64_t *>(hs_smem);  // [kHsStages]
   uint64_t *empty = full + kHsStages;                        // [kHsStages]
   int *item_id = reinterpret_cast<int *>(empty + kHsStages); // [kHsStages]
+  HsumParams *sp = reinterpret_cast<HsumParams *>(hs_smem + 16);  // copy for the emitter
   float *stages = hs_smem + 256;                             // 1 KB header
   EmitBuf &eb = *reinterpret_cast<EmitBuf *>(stages + kHsStages * p.stage_floats);
   constexpr int kRows1 = 4 * NW;
@@ -284,14 +366,18 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
     fence_mbar_init();
   }
   if (threadIdx.x < kMaxPlanes) eb.pc[threadIdx.x] = 0;
+  static_assert(sizeof(HsumParams) % 4 == 0 && 64 + sizeof(HsumParams) <= 1024, "header holds the parameters");
+  for (int i = threadIdx.x; i < (int)(sizeof(HsumParams) / 4); i += blockDim.x)
+    reinterpret_cast<int *>(sp)[i] = reinterpret_cast<const int *>(&p)[i];
   __syncthreads();
 
   if (warp == NW) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
-      // items are taken from the global counter in chunks of kChunk, and the
-      // next chunk is requested one chunk ahead so the atomic's latency is hidden
-      constexpr int kChunk = 2;
+      // items are taken from the global counter one at a time, the next one
+      // requested an item ahead so the atomic's latency is hidden (few items
+      // reserved per CTA keeps the end of the launch even)
+      constexpr int kChunk = 1;
       int cur = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
       int nxt = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
       int used = 0;
@@ -341,51 +427,16 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
       const float *stage = stages + st * p.stage_floats;
       // lane l holds bins f0 + 4 l + {0..3} and f0 + 128 + 4 l + {0..3}: the
       // lanes of a warp read consecutive 16-byte words (no bank conflicts)
-      const int Fl = 4 * lane;
-      const int F = f0 + Fl;
-      bool rowok[4];
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk) rowok[kk] = (t0 + kk <= H) && (t0 + kk >= item.tlo);
-      const bool tail = f0 + kHsBins > p.n_bins;
+      const int F = f0 + 4 * lane;
       float acc[4][8];
-      auto load_plane1 = [&]() {
-        const float *r1 = stage + p.soff[1] + Fl;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const float *rr = r1 + srow(t0 + kk, kRows1, sgn) * kHsBins;
-          const float4 q0 = *reinterpret_cast<const float4 *>(rr);
-          const float4 q1 = *reinterpret_cast<const float4 *>(rr + 128);
-          acc[kk][0] = q0.x; acc[kk][1] = q0.y; acc[kk][2] = q0.z; acc[kk][3] = q0.w;
-          acc[kk][4] = q1.x; acc[kk][5] = q1.y; acc[kk][6] = q1.z; acc[kk][7] = q1.w;
-          if (!rowok[kk]) {
-#pragma unroll
-            for (int e = 0; e < 8; ++e) acc[kk][e] = -CUDART_INF_F;
-          }
-        }
-        if (tail) {
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-#pragma unroll
-            for (int e = 0; e < 8; ++e)
-              if (F + (e & 3) + ((e >> 2) << 7) >= p.n_bins) acc[kk][e] = -CUDART_INF_F;
-        }
-      };
-      load_plane1();
-      auto emit = [&](int plane) {
-        Tile32 tile;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-#pragma unroll
-          for (int e = 0; e < 8; ++e) tile.v[8 * kk + e] = acc[kk][e];
-        emit_tile(eb, p, tile, plane, H, sgn, t0, F);
-      };
-      // rare: some lane of the warp reached the band of the plane (warp-uniform)
+      hs_load_plane1<NW>(acc, stage, p, f0, sgn, item.tlo, t0, F);
+      unsigned need = 0;  // planes (bit j - 1) where some lane reached the band; warp-uniform
       // ub: an upper bound of the lane's tile maximum.  Rounded addition is
       // monotone, so ub + (largest value added) bounds every new sum, and the
       // exact maximum (a 3-input max tree) is only needed where the bound reaches
       // a plane's band
       float ub = max32(acc);
-      if (__any_sync(0xffffffffu, ub >= p.trig[0])) emit(0);
+      if (__any_sync(0xffffffffu, ub >= p.trig[0])) need = 1u;
       hs_sfor<MAXP - 1>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value + 2;
         if (j <= P) {
@@ -454,10 +505,14 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           ub += vmax;
           if (__any_sync(0xffffffffu, ub >= p.trig[j - 1])) {
             ub = max32(acc);
-            if (__any_sync(0xffffffffu, ub >= p.trig[j - 1])) emit(j - 1);
+            if (__any_sync(0xffffffffu, ub >= p.trig[j - 1])) need |= 1u << (j - 1);
           }
         }
       });
+      if (need) {
+        if constexpr (MINB >= 2) hs_emit_item_body<NW>(p, stage, &eb, f0, sgn, item.tlo, t0, need);
+        else hs_emit_item<NW>(sp, stage, &eb, f0, sgn, item.tlo, t0, need);
+      }
 
       // release the stage to the producer
       __syncwarp();
