@@ -7,7 +7,10 @@ harmonic summing with chi-square thresholds (FAR 1e-6), FP64 recheck and the
 sorted candidate list.
 
 * ``value``: searches/s with the spectrum already resident in HBM
-  (fdas_enqueue_search_device), timed with CUDA events on the library's stream.
+  (fdas_enqueue_search_device), timed with CUDA events on the library's
+  streams; the best of three issue forms (``mode``): one buffer set
+  (sequential), searches alternating between sets A and B (alternating), and
+  A/B with the overlap configuration (pipelined); all three are reported.
 * ``e2e``: the same metric through the reference-facing call (fdas_launch /
   fdas_wait) with pinned HOST buffers: the 2^21-bin spectrum is copied in and
   the 4096-entry candidate list copied out inside every step.
@@ -293,17 +296,26 @@ def run_ours(args):
     counters = p.counters(FDAS.A)
     n_cand = sum(counters["per_plane"])
     dropped = max(0, n_cand - counters["records"])
-    # pipelined form: searches alternate between buffer sets A and B on their
-    # own streams; the kernels are sized so that the FT convolution of one
-    # search and the harmonic summing of the previous share every SM
+    # alternating form: the same handle, searches alternate between buffer
+    # sets A and B on their own streams, so one search's kernels start on the
+    # SMs the previous search's kernels release at their ends
+    with ClockSampler(local) as clocks_alt:
+        alt_ms, _ = timed_device_loop(p, [FDAS.A, FDAS.B], args.steps)
+    alt_ms = max_over_ranks(alt_ms)
+    # pipelined form: A/B as above with kernels sized so that the FT
+    # convolution of one search and the harmonic summing of the previous share
+    # every SM for their whole duration
     q = make_handle(True)
     with ClockSampler(local) as clocks:
         pipe_ms, _ = timed_device_loop(q, [FDAS.A, FDAS.B], args.steps)
     pipe_ms = max_over_ranks(pipe_ms)
-    total_ms = min(seq_ms, pipe_ms)
+    runs = {"sequential": (seq_ms, clocks_seq, p), "alternating": (alt_ms, clocks_alt, p),
+            "pipelined": (pipe_ms, clocks, q)}
+    mode = min(runs, key=lambda k: runs[k][0])
+    total_ms = runs[mode][0]
     value = ws * args.steps / (total_ms / 1e3)
-    mode = "pipelined" if pipe_ms <= seq_ms else "sequential"
-    clk = (clocks if mode == "pipelined" else clocks_seq).summary()  # clocks of the reported loop
+    clk = runs[mode][1].summary()  # clocks of the reported loop
+    mode_values = {f"value_{k}": ws * args.steps / (v[0] / 1e3) for k, v in runs.items()}
 
     # ---- stage times (separate pass, so the per-launch host syncs do not
     # disturb the throughput number above)
@@ -329,8 +341,7 @@ def run_ours(args):
     if args.no_e2e:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_bins": n_bins, "mode": mode,
-                              "value_sequential": ws * args.steps / (seq_ms / 1e3),
-                              "value_pipelined": ws * args.steps / (pipe_ms / 1e3),
+                              **mode_values,
                               "stage_ms": stage_ms, "counters": counters, "profile_run": True}), flush=True)
         return
     hx = {ab: PinnedArray((n_bins,), np.complex64) for ab in (FDAS.A, FDAS.B)}
@@ -340,7 +351,7 @@ def run_ours(args):
     hl = {ab: PinnedArray((n_list,), np.uint32) for ab in (FDAS.A, FDAS.B)}
     hp = {ab: PinnedArray((n_list,), np.float32) for ab in (FDAS.A, FDAS.B)}
     e2e_steps = args.steps
-    ep = q if mode == "pipelined" else p  # the faster configuration
+    ep = runs[mode][2]  # the faster configuration
     for i in range(args.warmup):
         ab = i & 1
         assert ep.launch(hx[ab].array, thr, hl[ab].array, hp[ab].array, FDAS.AllAccelerations, ab)
@@ -376,8 +387,7 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "mode": mode, "value_sequential": ws * args.steps / (seq_ms / 1e3),
-        "value_pipelined": ws * args.steps / (pipe_ms / 1e3),
+        "mode": mode, **mode_values,
         "dtype": "f32", "data": "synthetic", "config": dict(WORKLOAD, parallelism=f"replicas{ws}"),
         "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
         "stage_ms": stage_ms, "candidates": int(n_cand), "candidates_dropped": int(dropped),
