@@ -482,19 +482,37 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
             const float *r1 = r0 + sgn * bw;
             float c0[8], c1[8];
             // bins F + c and F + 128 + c (c < 4) sit at (F + c) / j = qa + (ra + c >= j)
-            // (ra + 3 < 2 j), and likewise for the second group: two divisions per plane
+            // (ra + 3 < 2 j), and likewise for the second group: two divisions per
+            // plane, and two staged values per group and row, qa and qa + 1
+            // (inside the box: bw >= 255 / j + 6)
             const int qa = F / j, ra = F - qa * j;
             const int qb = (F + 128) / j, rg = F + 128 - qb * j;
+            bool hi_a[4], hi_b[4];  // cell c takes the value at q + 1
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-              const int c = e & 3;
-              const int o = e < 4 ? qa + (ra + c >= j ? 1 : 0) : qb + (rg + c >= j ? 1 : 0);
-              c0[e] = r0[o];
-              c1[e] = kstar < 4 ? r1[o] : 0.f;  // the second row only where the four rows split
+            for (int c = 0; c < 4; ++c) {
+              hi_a[c] = ra + c >= j;
+              hi_b[c] = rg + c >= j;
             }
-            vmax = fmax3(fmax3(c0[0], c0[1], c0[2]), fmax3(c0[3], c0[4], c0[5]), fmaxf(c0[6], c0[7]));
-            if (kstar < 4)
-              vmax = fmax3(vmax, fmax3(fmax3(c1[0], c1[1], c1[2]), fmax3(c1[3], c1[4], c1[5]), c1[6]), c1[7]);
+            const float2 va = make_float2(r0[qa], r0[qa + 1]), vb = make_float2(r0[qb], r0[qb + 1]);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              c0[c] = hi_a[c] ? va.y : va.x;
+              c0[c + 4] = hi_b[c] ? vb.y : vb.x;
+            }
+            // the bound may include a value no cell takes: still an upper bound
+            vmax = fmaxf(fmaxf(va.x, va.y), fmaxf(vb.x, vb.y));
+            if (kstar < 4) {  // the second row only where the four rows split
+              const float2 wa = make_float2(r1[qa], r1[qa + 1]), wb = make_float2(r1[qb], r1[qb + 1]);
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                c1[c] = hi_a[c] ? wa.y : wa.x;
+                c1[c + 4] = hi_b[c] ? wb.y : wb.x;
+              }
+              vmax = fmax3(vmax, fmaxf(wa.x, wa.y), fmaxf(wb.x, wb.y));
+            } else {
+#pragma unroll
+              for (int e = 0; e < 8; ++e) c1[e] = 0.f;
+            }
             switch (kstar < 4 ? kstar : 4) {
               case 1: add_rows<1>(acc, c0, c1); break;
               case 2: add_rows<2>(acc, c0, c1); break;
@@ -525,6 +543,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
   if (threadIdx.x < P && eb.pc[threadIdx.x]) atomicAdd(p.cand_count + threadIdx.x, eb.pc[threadIdx.x]);
 }
 
+constexpr int kSelUnroll = 4;  // records per thread in flight in the selection passes
+constexpr int kRcUnroll = 8;   // taps per lane in flight in the FP64 recheck
+
 // FP64 recheck: a CTA per entry (grid-stride), warp j computes the FP64 FOP
 // cell FOP(trunc(t/(j+1)), bin/(j+1)) = |sum_q X[g - q] h_r[q]|^2
 // (ft_conv.py:201-205) with its lanes over the taps; warp 0 then sums the
@@ -545,12 +566,24 @@ __global__ void __launch_bounds__(512) recheck_kernel(RecheckParams p) {
       const int qn = min(p.tap_len[r], g + 1);
       const double2 *h = p.taps + (long long)r * p.tap_pitch;
       double re = 0.0, im = 0.0;
-#pragma unroll 4
-      for (int q = lane; q < qn; q += 32) {
-        const float2 x = p.input[g - q];
-        const double2 c = h[q];
-        re += (double)x.x * c.x - (double)x.y * c.y;
-        im += (double)x.x * c.y + (double)x.y * c.x;
+      // taps q = lane + 32 u in ascending order; the loads of a pass are all
+      // issued before the arithmetic, so one memory latency covers 256 taps
+      for (int q0 = 0; q0 < qn; q0 += 32 * kRcUnroll) {
+        float2 x[kRcUnroll];
+        double2 c[kRcUnroll];
+#pragma unroll
+        for (int u = 0; u < kRcUnroll; ++u) {
+          const int q = q0 + lane + 32 * u;
+          x[u] = q < qn ? p.input[g - q] : make_float2(0.f, 0.f);
+          c[u] = q < qn ? h[q] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < kRcUnroll; ++u) {
+          if (q0 + lane + 32 * u < qn) {
+            re += (double)x[u].x * c[u].x - (double)x[u].y * c[u].y;
+            im += (double)x[u].x * c[u].y + (double)x[u].y * c[u].x;
+          }
+        }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -588,23 +621,35 @@ __device__ __forceinline__ int pwr_bucket(float pw) { return (int)((__float_as_u
 __global__ void __launch_bounds__(1024) select_hist_kernel(SelectParams p) {
   extern __shared__ unsigned sh_hist[];  // [n_planes][kSelBuckets]
   __shared__ bool last;
+  __shared__ bool over[kMaxPlanes];  // plane has more hits than K
   const int nb = p.n_planes * kSelBuckets;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) sh_hist[i] = 0u;
+  if (threadIdx.x < kMaxPlanes)
+    over[threadIdx.x] = threadIdx.x < p.n_planes && p.cand_count[threadIdx.x] > (unsigned)p.per_plane;
   __syncthreads();
   const unsigned n = min(*p.cand_total, (unsigned)p.cand_cap);
-  const unsigned K = (unsigned)p.per_plane;
-  // warp-uniform loop; lanes that hit the same (plane, bucket) -- common, since
-  // a signal's hits have similar powers -- add once, through their leader
+  // warp-uniform loop, kSelUnroll records per lane in flight; lanes that hit
+  // the same (plane, bucket) -- common, since a signal's hits have similar
+  // powers -- add once, through their leader
   const unsigned ln = threadIdx.x & 31;
-  for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += gridDim.x * blockDim.x) {
-    const unsigned i = base + ln;
-    unsigned slot = 0xffffffffu;
-    if (i < n) {
-      const int plane = (int)(p.cand_key[i] >> 48);
-      if (p.cand_count[plane] > K) slot = (unsigned)(plane * kSelBuckets + pwr_bucket(p.cand_pwr[i]));
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += kSelUnroll * stride) {
+    unsigned long long k[kSelUnroll];
+    float w[kSelUnroll];
+#pragma unroll
+    for (int u = 0; u < kSelUnroll; ++u) {
+      const unsigned i = base + u * stride + ln;
+      k[u] = i < n ? p.cand_key[i] : ~0ull;
+      w[u] = i < n ? p.cand_pwr[i] : 0.f;
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, slot);
-    if (slot != 0xffffffffu && ln == (unsigned)(__ffs(peers) - 1)) atomicAdd(sh_hist + slot, (unsigned)__popc(peers));
+#pragma unroll
+    for (int u = 0; u < kSelUnroll; ++u) {
+      const int plane = (int)(k[u] >> 48);
+      const unsigned slot = (k[u] != ~0ull && over[plane]) ? (unsigned)(plane * kSelBuckets + pwr_bucket(w[u]))
+                                                            : 0xffffffffu;
+      const unsigned peers = __match_any_sync(0xffffffffu, slot);
+      if (slot != 0xffffffffu && ln == (unsigned)(__ffs(peers) - 1)) atomicAdd(sh_hist + slot, (unsigned)__popc(peers));
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nb; i += blockDim.x)
@@ -623,7 +668,8 @@ __global__ void __launch_bounds__(1024) select_hist_kernel(SelectParams p) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp < p.n_planes) {
     const int plane = warp;
-    if (p.cand_count[plane] <= K) {
+    const unsigned K = (unsigned)p.per_plane;
+    if (!over[plane]) {
       if (lane == 0) p.sel_bucket[plane] = -1;
     } else {
       const unsigned *h = sh_hist + plane * kSelBuckets;
@@ -651,25 +697,41 @@ __global__ void __launch_bounds__(1024) select_hist_kernel(SelectParams p) {
 }
 
 __global__ void __launch_bounds__(256) select_gather_kernel(SelectParams p) {
+  __shared__ int sb_of[kMaxPlanes];
+  if (threadIdx.x < kMaxPlanes) sb_of[threadIdx.x] = threadIdx.x < p.n_planes ? p.sel_bucket[threadIdx.x] : -1;
+  __syncthreads();
   const unsigned n = min(*p.cand_total, (unsigned)p.cand_cap);
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const unsigned long long key = p.cand_key[i];
-    const int plane = (int)(key >> 48);
-    const float pw = p.cand_pwr[i];
-    const int sb = p.sel_bucket[plane];
-    const int b = pwr_bucket(pw);
-    int list = -1;
-    unsigned *cnt = nullptr;
-    if (sb < 0 || b > sb) { list = 0; cnt = p.sure_count + plane; }
-    else if (b == sb) { list = 1; cnt = p.bound_count + plane; }
-    if (list >= 0) {
-      const unsigned idx = atomicAdd(cnt, 1u);
-      if (idx < (unsigned)kSortCap) {
-        const size_t o = ((size_t)plane * 2 + list) * kSortCap + idx;
-        p.sel_key[o] = key;
-        p.sel_pwr[o] = pw;
-      } else {
-        atomicOr(p.status, kStatusSelectionOverflow);
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kSelUnroll * stride) {
+    unsigned long long k[kSelUnroll];
+    float w[kSelUnroll];
+#pragma unroll
+    for (int u = 0; u < kSelUnroll; ++u) {
+      const unsigned i = base + u * stride;
+      k[u] = i < n ? p.cand_key[i] : ~0ull;
+      w[u] = i < n ? p.cand_pwr[i] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < kSelUnroll; ++u) {
+      if (k[u] == ~0ull) continue;
+      const unsigned long long key = k[u];
+      const int plane = (int)(key >> 48);
+      const float pw = w[u];
+      const int sb = sb_of[plane];
+      const int b = pwr_bucket(pw);
+      int list = -1;
+      unsigned *cnt = nullptr;
+      if (sb < 0 || b > sb) { list = 0; cnt = p.sure_count + plane; }
+      else if (b == sb) { list = 1; cnt = p.bound_count + plane; }
+      if (list >= 0) {
+        const unsigned idx = atomicAdd(cnt, 1u);
+        if (idx < (unsigned)kSortCap) {
+          const size_t o = ((size_t)plane * 2 + list) * kSortCap + idx;
+          p.sel_key[o] = key;
+          p.sel_pwr[o] = pw;
+        } else {
+          atomicOr(p.status, kStatusSelectionOverflow);
+        }
       }
     }
   }
@@ -775,7 +837,7 @@ cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s) 
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
-  recheck_kernel<<<2 * 152, 32 * 8, 0, s>>>(p);
+  recheck_kernel<<<4 * 152, 32 * 8, 0, s>>>(p);
   return cudaGetLastError();
 }
 
