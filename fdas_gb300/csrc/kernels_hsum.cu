@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
       // exact maximum (a 3-input max tree) is only needed where the bound reaches
       // a plane's band
       float ub = max32(acc);
-      if (__any_sync(0xffffffffu, ub >= p.trig[0])) need = 1u;
+      unsigned need_lane = ub >= p.trig[0] ? 1u : 0u;  // this lane's marks; one vote per item
       hs_sfor<MAXP - 1>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value + 2;
         if (j <= P) {
@@ -521,12 +521,13 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
             }
           }
           ub += vmax;
-          if (__any_sync(0xffffffffu, ub >= p.trig[j - 1])) {
+          if (ub >= p.trig[j - 1]) {  // per lane: no vote, no warp-wide branch in the plane loop
             ub = max32(acc);
-            if (__any_sync(0xffffffffu, ub >= p.trig[j - 1])) need |= 1u << (j - 1);
+            if (ub >= p.trig[j - 1]) need_lane |= 1u << (j - 1);
           }
         }
       });
+      need = __reduce_or_sync(0xffffffffu, need_lane);
       if (need) {
         if constexpr (MINB >= 2) hs_emit_item_body<NW>(p, stage, &eb, f0, sgn, item.tlo, t0, need);
         else hs_emit_item<NW>(sp, stage, &eb, f0, sgn, item.tlo, t0, need);
