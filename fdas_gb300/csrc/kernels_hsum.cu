@@ -614,8 +614,9 @@ __global__ void __launch_bounds__(512) recheck_kernel(RecheckParams p) {
 // plane's powers over 2048 buckets (float bits 30..20, powers are >= 0) built
 // in shared memory per CTA; the last CTA finds the bucket where the count from
 // the top reaches K; the records above it ("sure") and in it ("boundary") are
-// gathered; one CTA per plane ranks the boundary records and then orders the
-// kept ones by location, both by direct rank computation.
+// gathered; kFinSlices CTAs per plane each rank the boundary records and then
+// order their slice of the kept ones by location, both by direct rank
+// computation.
 
 __device__ __forceinline__ int pwr_bucket(float pw) { return (int)((__float_as_uint(pw) >> 20) & 0x7ffu); }
 
@@ -738,6 +739,8 @@ __global__ void __launch_bounds__(256) select_gather_kernel(SelectParams p) {
   }
 }
 
+constexpr int kFinSlices = 8;  // CTAs per plane in the finalize (slices of the K entries)
+
 // "a is stronger than b": power descending, key ascending on ties
 __device__ __forceinline__ bool stronger(float pa, unsigned long long ka, float pb, unsigned long long kb) {
   return pa > pb || (pa == pb && ka < kb);
@@ -781,17 +784,26 @@ __global__ void __launch_bounds__(1024) select_finalize_kernel(SelectParams p) {
   const int kept = keep_a + c;
   uint32_t *cl = p.compat_loc + (size_t)plane * K;
   float *cp = p.compat_pwr + (size_t)plane * K;
-  // order the kept records by location: position = number of smaller keys
-  for (int i = threadIdx.x; i < kept; i += blockDim.x) {
+  // this CTA's slice [lo, hi) of the K entries: the kept records i in it are
+  // placed, the unused positions in it (i >= kept) padded
+  const int per = (K + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int lo = (int)blockIdx.y * per, hi = min(K, lo + per);
+  // order the kept records by location: position = number of smaller keys,
+  // counted by a warp per record (lanes over the other records)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int i = lo + warp; i < min(hi, kept); i += nwarps) {
     const unsigned long long ki = fin[i];
-    int pos = 0;
-    for (int j = 0; j < kept; ++j) pos += fin[j] < ki;
-    const unsigned row = (unsigned)(ki >> 32) & 0xffffu, bin = (unsigned)(ki & 0xffffffffu);
-    // gen_info.h:62-64: ((h-1)&7)<<29 | (row&0x7f)<<22 | (bin&0x3fffff)
-    cl[pos] = (((unsigned)plane & 7u) << 29) | ((row & 0x7fu) << 22) | (bin & 0x3fffffu);
-    cp[pos] = finp[i];
+    unsigned pos = 0;
+    for (int j = lane; j < kept; j += 32) pos += fin[j] < ki ? 1u : 0u;
+    pos = __reduce_add_sync(0xffffffffu, pos);
+    if (lane == 0) {
+      const unsigned row = (unsigned)(ki >> 32) & 0xffffu, bin = (unsigned)(ki & 0xffffffffu);
+      // gen_info.h:62-64: ((h-1)&7)<<29 | (row&0x7f)<<22 | (bin&0x3fffff)
+      cl[pos] = (((unsigned)plane & 7u) << 29) | ((row & 0x7fu) << 22) | (bin & 0x3fffffu);
+      cp[pos] = finp[i];
+    }
   }
-  for (int i = kept + threadIdx.x; i < K; i += blockDim.x) {
+  for (int i = max(lo, kept) + (int)threadIdx.x; i < hi; i += blockDim.x) {
     cl[i] = p.invalid_location;
     cp[i] = -1.0f;
   }
@@ -858,7 +870,7 @@ cudaError_t launch_select(const SelectParams &p, cudaStream_t s) {
   const int fsmem = (kSortCap + kMaxCompat) * (8 + 4);
   e = cudaFuncSetAttribute(select_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, fsmem);
   if (e != cudaSuccess) return e;
-  select_finalize_kernel<<<p.n_planes, 1024, fsmem, s>>>(p);
+  select_finalize_kernel<<<dim3(p.n_planes, kFinSlices), 1024, fsmem, s>>>(p);
   return cudaGetLastError();
 }
 
