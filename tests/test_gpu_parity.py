@@ -122,6 +122,35 @@ def test_hsum_injected_fop_bit_exact(name, thr_key):
     assert np.array_equal(pwr, g["det_pwr_ref" + thr_key])
 
 
+@pytest.mark.parametrize("n_templates,n_planes", [(101, 16), (85, 16), (101, 8)])
+def test_hsum_injected_wide_bank_dense_hits(n_templates, n_planes):
+    """Banks wider than 88 rows (the 16-warp harmonic-summing variant) and 16
+    planes, on an injected FOP with patches that make most cells of some tiles
+    hits in every plane (the emission path at full load) and a ragged last
+    block: every hit and its power equal hsum.py's recurrence in float32."""
+    n = 6000
+    rng = np.random.default_rng(n_templates + n_planes)
+    fop = rng.exponential(1.0, size=(n_templates, n)).astype(np.float32)
+    half = n_templates // 2
+    fop[half - 12:half + 13, 300:340] *= np.float32(6.0)
+    fop[half - 4:half + 5, 2000:2012] = np.float32(300.0)
+    fop[:, n - 3:] = np.float32(90.0)  # the last bins, partly in the ragged block
+    k = np.arange(1, n_planes + 1)
+    thr = (k + 6.0 * np.sqrt(k) + 10.0).astype(np.float32)
+    p = make_pipeline(n, log=io.StringIO(), n_templates=n_templates, n_planes=n_planes)
+    assert p.inject_FOP(fop, FDAS.A), p.last_error
+    assert p.perform_harmonic_summing(thr, FDAS.AllAccelerations, FDAS.A), p.last_error
+    rec, total, dropped = p.retrieve_candidate_list(FDAS.A)
+    assert dropped == 0
+    hps = O.harmonic_planes(fop, n_planes=n_planes, dtype=np.float32)
+    _, pwr, plane, row, fbin = O.detections(hps, thr)
+    assert total == pwr.size and pwr.size > 10000
+    got = sorted(zip(rec["harmonic"].tolist(), rec["template_num"].tolist(), rec["bin"].tolist(),
+                     rec["power"].astype(np.float32).tolist()))
+    want = sorted(zip((plane + 1).tolist(), (row - half).tolist(), fbin.tolist(), pwr.tolist()))
+    assert got == want
+
+
 @pytest.mark.parametrize("part", [FDAS.NegativeAccelerations, FDAS.PositiveAccelerations])
 def test_hsum_injected_half_gtest_check(part):
     """The reference's Harmonic_Summing test (main_gtest.cpp:261-283)."""
