@@ -1188,12 +1188,14 @@ fdas_status fdas_host_unregister(void *ptr) {
 // ===========================================================================
 // Batched search (fdas_batch_*): many trials of uneven length in one pass.
 //
-// All trials' tiles are transformed by one tiling launch and all (trial, tile,
-// template) items by one persistent FT-convolution launch (the trial of a
-// global tile is found from a table of tile ranges), into one FOP arena with
-// each trial's FOP at its own offset.  Harmonic summing, FP64 recheck and
-// candidate selection then run per trial -- through "views", FDAS handles that
-// borrow the batch's buffers -- on a few branch streams.  The whole sequence
+// All trials' tiles are transformed by one tiling launch and the (trial, tile,
+// template) items by a few persistent FT-convolution launches over consecutive
+// groups of trials (the trial of a global tile is found from a table of tile
+// ranges), into one FOP arena with each trial's FOP at its own offset.
+// Harmonic summing, FP64 recheck and candidate selection run per trial --
+// through "views", FDAS handles that borrow the batch's buffers -- on branch
+// streams, each group's as soon as its FOPs are written, alongside the next
+// group's FT convolution.  The whole sequence
 // is captured once into a CUDA graph and replayed; before capture an
 // autotuner times the FFT split of the FT convolution (one warp, 64 x 32, or a
 // warp pair, 32 x 64), its CTAs per SM, and the harmonic-summing pipeline
@@ -1218,7 +1220,8 @@ struct fdas_batch {
   std::vector<fdas_handle *> views;
   cudaStream_t main = nullptr;
   std::vector<cudaStream_t> branch;
-  cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  std::vector<cudaEvent_t> forks;  // end of each group's FT convolution
   std::vector<cudaEvent_t> joins;
   cudaGraphExec_t exec = nullptr;
   std::vector<float> graph_thr;
@@ -1230,7 +1233,11 @@ struct fdas_batch {
 
 namespace {
 
-constexpr int kBatchBranches = 4;
+constexpr int kBatchBranches = 8;  // streams for the per-trial harmonic summing
+// The FT convolution runs as this many launches over consecutive groups of
+// trials; a group's harmonic summing starts on the branch streams as soon as
+// its FOPs are written, while the next group's FT convolution runs.
+constexpr int kBatchGroups = 16;
 constexpr int kBatchRecheckCap = 8192;
 
 fdas_status bfail(fdas_batch *b, fdas_status st, const std::string &msg) {
@@ -1264,7 +1271,7 @@ void batch_free(fdas_batch *b) {
   cudaFreeHost(b->h_status);
   for (auto s : b->branch) cudaStreamDestroy(s);
   for (auto e : b->joins) cudaEventDestroy(e);
-  if (b->fork) cudaEventDestroy(b->fork);
+  for (auto e : b->forks) cudaEventDestroy(e);
   if (b->t0) cudaEventDestroy(b->t0);
   if (b->t1) cudaEventDestroy(b->t1);
   if (b->main) cudaStreamDestroy(b->main);
@@ -1301,14 +1308,28 @@ fdas_status batch_enqueue(fdas_batch *b, const float *thr) {
   fp.variant = b->ftc_variant;
   fp.trials = b->d_trials;
   fp.n_trials = b->n_trials;
-  BCK(b, launch_ftc(fp, b->main));
-  BCK(b, cudaEventRecord(b->fork, b->main));
-  for (auto s : b->branch) BCK(b, cudaStreamWaitEvent(s, b->fork, 0));
-  for (int i = 0; i < b->n_trials; ++i) {
-    fdas_handle *v = b->views[i];
-    v->cfg.overlap = (uint32_t)b->hsum_lean;  // the lean harmonic-summing kernel
-    fdas_status st = enqueue_hsum(v, 0, thr, FDAS_ALL_ACCELERATIONS);
-    if (st != FDAS_OK) return bfail(b, st, v->err);
+  // groups of consecutive trials with about equal numbers of tiles
+  int i0 = 0;
+  for (int g = 0; g < (int)b->forks.size() && i0 < b->n_trials; ++g) {
+    const long long target = b->total_tiles * (g + 1) / (long long)b->forks.size();
+    int i1 = i0 + 1;
+    while (i1 < b->n_trials && (g + 1 == (int)b->forks.size() || b->trials[i1].tile_begin < target)) ++i1;
+    const long long t_lo = b->trials[i0].tile_begin;
+    const long long t_hi = i1 < b->n_trials ? b->trials[i1].tile_begin : b->total_tiles;
+    FtcParams gp = fp;
+    gp.tiles = b->d_tiles + (size_t)t_lo * kTile;
+    gp.n_tiles = (int)(t_hi - t_lo);
+    gp.tile_begin = t_lo;
+    BCK(b, launch_ftc(gp, b->main));
+    BCK(b, cudaEventRecord(b->forks[g], b->main));
+    for (auto s : b->branch) BCK(b, cudaStreamWaitEvent(s, b->forks[g], 0));
+    for (int i = i0; i < i1; ++i) {
+      fdas_handle *v = b->views[i];
+      v->cfg.overlap = (uint32_t)b->hsum_lean;  // the lean harmonic-summing kernel
+      fdas_status st = enqueue_hsum(v, 0, thr, FDAS_ALL_ACCELERATIONS);
+      if (st != FDAS_OK) return bfail(b, st, v->err);
+    }
+    i0 = i1;
   }
   for (size_t k = 0; k < b->branch.size(); ++k) {
     BCK(b, cudaEventRecord(b->joins[k], b->branch[k]));
@@ -1492,12 +1513,19 @@ fdas_status fdas_batch_create(const fdas_batch_config *cfg, const fdas_complex *
       (e = cudaHostAlloc((void **)&b->h_ctrl, sizeof(unsigned) * n * kCtrlWords, cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaHostAlloc((void **)&b->h_status, sizeof(int), cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess ||
       (e = cudaEventCreate(&b->t0)) != cudaSuccess || (e = cudaEventCreate(&b->t1)) != cudaSuccess) {
     batch_free(b);
     return bfail(nullptr, FDAS_ERR_CUDA, std::string("batch setup: ") + cudaGetErrorString(e));
   }
   *b->h_status = 0;
+  for (int g = 0; g < kBatchGroups; ++g) {
+    cudaEvent_t ev = nullptr;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      batch_free(b);
+      return bfail(nullptr, FDAS_ERR_CUDA, "batch events");
+    }
+    b->forks.push_back(ev);
+  }
   for (int k = 0; k < kBatchBranches; ++k) {
     cudaStream_t s = nullptr;
     cudaEvent_t ev = nullptr;

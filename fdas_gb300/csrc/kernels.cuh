@@ -84,6 +84,7 @@ struct FtcParams {
                           // 3 / 4: tensor-core DFT factors with split BF16 / FP16 operands
   const BatchTrial *trials = nullptr;  // batched search: tiles of all trials, FOPs per trial
   int n_trials = 0;
+  long long tile_begin = 0;  // batched search: global index of the launch's first tile
 };
 
 // ---- (d) harmonic summing + thresholds + candidate compaction (preload,

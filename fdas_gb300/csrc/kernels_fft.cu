@@ -100,13 +100,20 @@ struct FopTarget {
   long long base;
   int n_bins;
 };
+// Trial of the launch's tile `tile` (batched search; 0 otherwise).  Looked up
+// when the item starts, so the search's dependent loads overlap the FFT.
 template <bool BATCH>
-__device__ __forceinline__ FopTarget fop_target(const FtcParams &p, int tile, int row) {
+__device__ __forceinline__ int trial_of(const FtcParams &p, int tile) {
+  if constexpr (!BATCH) return 0;
+  return batch_trial_of(p.trials, p.n_trials, p.tile_begin + tile);  // the launch may cover a range of tiles
+}
+template <bool BATCH>
+__device__ __forceinline__ FopTarget fop_target(const FtcParams &p, int tile, int row, int trial) {
   if constexpr (!BATCH)
     return FopTarget{p.fop + (long long)row * p.fop_stride, (long long)tile * p.payload - p.overlap, p.n_bins};
-  const BatchTrial &tr = p.trials[batch_trial_of(p.trials, p.n_trials, tile)];
+  const BatchTrial &tr = p.trials[trial];
   return FopTarget{p.fop + tr.fop_offset + (long long)row * tr.stride,
-                   (tile - tr.tile_begin) * p.payload - p.overlap, tr.n_bins};
+                   (p.tile_begin + tile - tr.tile_begin) * p.payload - p.overlap, tr.n_bins};
 }
 
 // Persistent: one CTA of 8 warps per SM; each warp loops over (tile,
@@ -143,6 +150,7 @@ __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
   for (; item < n_items; item += stride) {
     const int tile = item / p.n_rows;
     const int row = p.row_begin + (item - tile * p.n_rows);
+    const int trial = trial_of<BATCH>(p, tile);
     const float2 *s = p.tiles + (long long)tile * kTile + lane;
     float2 v[64];
     sfor<64>([&](auto K) {
@@ -165,7 +173,7 @@ __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
       if (next < n_items && lane == 0)
         prefetch_template(ex, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
     });
-    const FopTarget tg = fop_target<BATCH>(p, tile, row);
+    const FopTarget tg = fop_target<BATCH>(p, tile, row, trial);
     sfor<2>([&](auto C) {
       constexpr int c = decltype(C)::value;
       sfor<32>([&](auto D) {
@@ -232,6 +240,7 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
   for (; item < n_items; item += stride) {
     const int tile = item / p.n_rows;
     const int row = p.row_begin + (item - tile * p.n_rows);
+    const int trial = trial_of<BATCH>(p, tile);
     const float2 *s = p.tiles + (long long)tile * kTile + tp;
     float2 v[32];
     sfor<32>([&](auto A) {
@@ -259,7 +268,7 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
       if (next < n_items && tp == 0)
         prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
     });
-    const FopTarget tg = fop_target<BATCH>(p, tile, row);
+    const FopTarget tg = fop_target<BATCH>(p, tile, row, trial);
     sfor<4>([&](auto R) {
       constexpr int r = decltype(R)::value;
       sfor<8>([&](auto D2) {
