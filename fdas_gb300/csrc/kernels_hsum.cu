@@ -405,10 +405,13 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
         float *stage = stages + st * p.stage_floats;
         mbar_arrive_expect_tx(full + st, p.stage_bytes);
         tma_load_2d(stage + p.soff[1], &m.map[1], item.f0, item.sgn > 0 ? H : H - (kRows1 - 1), full + st);
-        for (int j = 2; j <= P; ++j) {
-          const int a0 = (item.f0 / j) & ~3;
-          tma_load_2d(stage + p.soff[j], &m.map[j], a0, item.sgn > 0 ? H : H - (p.bh[j] - 1), full + st);
-        }
+        hs_sfor<MAXP - 1>([&](auto JJ) {  // j known at compile time: divisions by constants
+          constexpr int j = decltype(JJ)::value + 2;
+          if (j <= P) {
+            const int a0 = (item.f0 / j) & ~3;
+            tma_load_2d(stage + p.soff[j], &m.map[j], a0, item.sgn > 0 ? H : H - (p.bh[j] - 1), full + st);
+          }
+        });
       }
     }
   } else {
