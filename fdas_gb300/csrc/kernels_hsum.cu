@@ -346,10 +346,14 @@ template <int MAXP, int NW, int kHsStages, int MINB>
 __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_constant__ HsumParams p,
                                                                     const __grid_constant__ HsumMaps m) {
   extern __shared__ __align__(1024) float hs_smem[];
+  // per stage: `full` completes when the plane-1 box has landed, `full2` when
+  // the sub-harmonic boxes have, so the consumers start on plane 1 while the
+  // rest of the stage is still arriving
   uint64_t *full = reinterpret_cast<uint64_t *>(hs_smem);  // [kHsStages]
-  uint64_t *empty = full + kHsStages;                        // [kHsStages]
+  uint64_t *full2 = full + kHsStages;                        // [kHsStages]
+  uint64_t *empty = full2 + kHsStages;                       // [kHsStages]
   int *item_id = reinterpret_cast<int *>(empty + kHsStages); // [kHsStages]
-  HsumParams *sp = reinterpret_cast<HsumParams *>(hs_smem + 16);  // copy for the emitter
+  HsumParams *sp = reinterpret_cast<HsumParams *>(hs_smem + 32);  // copy for the emitter
   float *stages = hs_smem + 256;                             // 1 KB header
   EmitBuf &eb = *reinterpret_cast<EmitBuf *>(stages + kHsStages * p.stage_floats);
   constexpr int kRows1 = 4 * NW;
@@ -361,12 +365,14 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
   if (threadIdx.x == 0) {
     for (int s = 0; s < kHsStages; ++s) {
       mbar_init(full + s, 1);
+      mbar_init(full2 + s, 1);
       mbar_init(empty + s, NW);
     }
     fence_mbar_init();
   }
   if (threadIdx.x < kMaxPlanes) eb.pc[threadIdx.x] = 0;
-  static_assert(sizeof(HsumParams) % 4 == 0 && 64 + sizeof(HsumParams) <= 1024, "header holds the parameters");
+  static_assert(sizeof(HsumParams) % 4 == 0 && 128 + sizeof(HsumParams) <= 1024, "header holds the parameters");
+  static_assert(kHsStages * (3 * 8 + 4) <= 128, "barriers and item ids before the parameter copy");
   for (int i = threadIdx.x; i < (int)(sizeof(HsumParams) / 4); i += blockDim.x)
     reinterpret_cast<int *>(sp)[i] = reinterpret_cast<const int *>(&p)[i];
   __syncthreads();
@@ -403,13 +409,15 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
         item_id[st] = it;
         const HsItem item = hs_item(p, it);
         float *stage = stages + st * p.stage_floats;
-        mbar_arrive_expect_tx(full + st, p.stage_bytes);
+        const unsigned bytes1 = (unsigned)(p.bw[1] * p.bh[1]) * 4u;
+        mbar_arrive_expect_tx(full + st, bytes1);
         tma_load_2d(stage + p.soff[1], &m.map[1], item.f0, item.sgn > 0 ? H : H - (kRows1 - 1), full + st);
+        mbar_arrive_expect_tx(full2 + st, p.stage_bytes - bytes1);  // 0 bytes with one plane: a plain arrival
         hs_sfor<MAXP - 1>([&](auto JJ) {  // j known at compile time: divisions by constants
           constexpr int j = decltype(JJ)::value + 2;
           if (j <= P) {
             const int a0 = (item.f0 / j) & ~3;
-            tma_load_2d(stage + p.soff[j], &m.map[j], a0, item.sgn > 0 ? H : H - (p.bh[j] - 1), full + st);
+            tma_load_2d(stage + p.soff[j], &m.map[j], a0, item.sgn > 0 ? H : H - (p.bh[j] - 1), full2 + st);
           }
         });
       }
@@ -440,6 +448,10 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
       // a plane's band
       float ub = max32(acc);
       unsigned need_lane = ub >= p.trig[0] ? 1u : 0u;  // this lane's marks; one vote per item
+      if (!mbar_wait_parity(full2 + st, use & 1, p.timeout_ns)) {
+        if (lane == 0) atomicOr(p.status, kStatusHsumTimeout);
+        break;
+      }
       hs_sfor<MAXP - 1>([&](auto JJ) {
         constexpr int j = decltype(JJ)::value + 2;
         if (j <= P) {
