@@ -382,10 +382,11 @@ void fdas_server_destroy(fdas_server *s);
 /* ------------------------------------------------------------------------
  * Batched search (no counterpart in the reference; the batched form).  Many
  * trials (dedispersed spectra) of uneven length searched in one pass: one
- * tiling launch and one persistent FT-convolution launch over the (trial,
- * tile, template) items of all trials, then harmonic summing, FP64 recheck
- * and candidate selection per trial on parallel branch streams; the sequence
- * is captured once into a CUDA graph and replayed.  Before the capture an
+ * tiling launch and persistent FT-convolution launches over the (trial, tile,
+ * template) items of consecutive groups of trials, each group's harmonic
+ * summing, FP64 recheck and candidate selection per trial on parallel branch
+ * streams while the next group's FT convolution runs; the sequence is
+ * captured once into a CUDA graph and replayed.  Before the capture an
  * autotuner (cfg->autotune) times the FT convolution's FFT split (one warp,
  * 64 x 32, or a warp pair, 32 x 64), its CTAs per SM and the harmonic-summing
  * pipeline depth on the batch itself and keeps the fastest.  Every trial gets
