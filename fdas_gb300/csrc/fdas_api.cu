@@ -46,7 +46,7 @@ struct BufferSet {
   const float2 *cur_input = nullptr;
   float2 *d_tiles = nullptr;
   float2 *d_tmpl = nullptr;
-  double2 *d_taps = nullptr;
+  double2 *d_taps = nullptr;  // FP64 taps while templates are uploaded, then float pairs (split_taps)
   int *d_taplen = nullptr;
   float *d_fop = nullptr;
   unsigned long long *d_key = nullptr;
@@ -351,7 +351,7 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
     r.input = S.cur_input;
     r.n_bins = h->N;
     r.half = H;
-    r.taps = S.d_taps + (size_t)h->row0 * h->tap_pitch;
+    r.taps = reinterpret_cast<const float4 *>(S.d_taps + (size_t)h->row0 * h->tap_pitch);
     r.tap_len = S.d_taplen + h->row0;
     r.tap_pitch = h->tap_pitch;
     for (int j = 0; j < kMaxPlanes; ++j) r.thr[j] = j < P ? (double)thr[j] : INFINITY;
@@ -747,6 +747,9 @@ fdas_status fdas_upload_templates(fdas_handle *h, const fdas_complex *templates,
   } else {
     return fail(h, FDAS_ERR_INVALID_ARG, "unknown template layout");
   }
+  // the recheck reads the taps as hi + lo float pairs (FP32-pipe products)
+  CK(h, launch_split_taps(d_taps, (long long)T * h->tap_pitch, S.stream));
+  CK(h, cudaStreamSynchronize(S.stream));
   S.have_templates = true;
   S.have_taps = true;
   if (S.taplen.size() < (size_t)h->alloc_T) S.taplen.assign(h->alloc_T, 0);

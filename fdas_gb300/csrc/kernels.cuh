@@ -130,7 +130,8 @@ struct RecheckParams {
   const float2 *input;    // the spectrum the FOP was computed from
   int n_bins;
   int half;
-  const double2 *taps;    // n_templates x tap_pitch time-domain taps (FP64)
+  const float4 *taps;     // n_templates x tap_pitch time-domain taps as float pairs
+                          // (re hi, im hi, re lo, im lo): tap = hi + lo to 2^-48
   const int *tap_len;     // taps per template
   int tap_pitch;
   double thr[kMaxPlanes];
@@ -208,6 +209,7 @@ cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s);
 // consumer warps of the harmonic-summing kernel for `half` (4 templates each)
 int hsum_warps(int half);
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s);
+cudaError_t launch_split_taps(double2 *taps, long long n, cudaStream_t s);
 cudaError_t launch_select(const SelectParams &p, cudaStream_t s);
 cudaError_t launch_spectra(const SpectraParams &p, cudaStream_t s);
 cudaError_t launch_taps(const TapsParams &p, cudaStream_t s);

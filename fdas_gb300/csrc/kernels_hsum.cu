@@ -562,10 +562,38 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
 constexpr int kSelUnroll = 4;  // records per thread in flight in the selection passes
 constexpr int kRcUnroll = 8;   // taps per lane in flight in the FP64 recheck
 
-// FP64 recheck: a CTA per entry (grid-stride), warp j computes the FP64 FOP
+// FP64 taps -> float pairs in place: (re hi, im hi, re lo, im lo) with
+// hi = fl32(c), lo = fl32(c - hi), so c = hi + lo to 2^-48 relative.  The
+// recheck then forms its products on the FP32 pipe; GB300's FP64 rate is
+// about 1/64 of its FP32 rate.
+__global__ void split_taps_kernel(double2 *taps, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 c = taps[i];
+    const float hr = __double2float_rn(c.x), hm = __double2float_rn(c.y);
+    const float lr = __double2float_rn(c.x - (double)hr), lm = __double2float_rn(c.y - (double)hm);
+    reinterpret_cast<float4 *>(taps)[i] = make_float4(hr, hm, lr, lm);
+  }
+}
+
+// (s, t) += a (bh + bl) in double-float arithmetic: a bh = p + pe exactly
+// (FMA), s + p = u + e exactly (Knuth's two-sum), the small terms gathered in
+// t.  Rounded intrinsics keep the compiler from fusing the error-free steps.
+__device__ __forceinline__ void df_add_prod(float &s, float &t, float a, float bh, float bl) {
+  const float pr = __fmul_rn(a, bh);
+  const float pe = fmaf(a, bh, -pr);
+  const float u = __fadd_rn(s, pr);
+  const float bb = __fsub_rn(u, s);
+  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(u, bb)), __fsub_rn(pr, bb));
+  t = __fadd_rn(t, __fadd_rn(e, fmaf(a, bl, pe)));
+  s = u;
+}
+
+// FP64-grade recheck: a CTA per entry (grid-stride), warp j computes the FOP
 // cell FOP(trunc(t/(j+1)), bin/(j+1)) = |sum_q X[g - q] h_r[q]|^2
-// (ft_conv.py:201-205) with its lanes over the taps; warp 0 then sums the
-// planes in order j = 1..k (hsum.py:95-120) and compares with the threshold.
+// (ft_conv.py:201-205) with its lanes over the taps -- per lane in
+// double-float arithmetic (about 2^-44 relative), then in FP64 across the
+// lanes; warp 0 sums the planes in order j = 1..k (hsum.py:95-120) in FP64
+// and compares with the threshold.
 __global__ void __launch_bounds__(512) recheck_kernel(RecheckParams p) {
   __shared__ double cell[kMaxPlanes];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -580,27 +608,31 @@ __global__ void __launch_bounds__(512) recheck_kernel(RecheckParams p) {
       const int r = p.half + tj;
       const int g = bin / j;
       const int qn = min(p.tap_len[r], g + 1);
-      const double2 *h = p.taps + (long long)r * p.tap_pitch;
-      double re = 0.0, im = 0.0;
+      const float4 *h = p.taps + (long long)r * p.tap_pitch;
+      float rs = 0.f, rt = 0.f, is = 0.f, it = 0.f;  // double-float sums of re and im
       // taps q = lane + 32 u in ascending order; the loads of a pass are all
       // issued before the arithmetic, so one memory latency covers 256 taps
       for (int q0 = 0; q0 < qn; q0 += 32 * kRcUnroll) {
         float2 x[kRcUnroll];
-        double2 c[kRcUnroll];
+        float4 c[kRcUnroll];
 #pragma unroll
         for (int u = 0; u < kRcUnroll; ++u) {
           const int q = q0 + lane + 32 * u;
           x[u] = q < qn ? p.input[g - q] : make_float2(0.f, 0.f);
-          c[u] = q < qn ? h[q] : make_double2(0.0, 0.0);
+          c[u] = q < qn ? h[q] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < kRcUnroll; ++u) {
           if (q0 + lane + 32 * u < qn) {
-            re += (double)x[u].x * c[u].x - (double)x[u].y * c[u].y;
-            im += (double)x[u].x * c[u].y + (double)x[u].y * c[u].x;
+            // re += x.re c.re - x.im c.im, im += x.re c.im + x.im c.re
+            df_add_prod(rs, rt, x[u].x, c[u].x, c[u].z);
+            df_add_prod(rs, rt, -x[u].y, c[u].y, c[u].w);
+            df_add_prod(is, it, x[u].x, c[u].y, c[u].w);
+            df_add_prod(is, it, x[u].y, c[u].x, c[u].z);
           }
         }
       }
+      double re = (double)rs + (double)rt, im = (double)is + (double)it;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         re += __shfl_xor_sync(0xffffffffu, re, o);
@@ -862,6 +894,13 @@ cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s) 
     return launch_hsum_t<16, 11, 2, 1>(p, m, s);
   }
   return launch_hsum_t<16, 16, 2, 1>(p, m, s);
+}
+
+cudaError_t launch_split_taps(double2 *taps, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = (n + 255) / 256;
+  split_taps_kernel<<<(int)(blocks < 1024 ? blocks : 1024), 256, 0, s>>>(taps, n);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
