@@ -93,7 +93,7 @@ typedef struct {
   int32_t device;              /* CUDA device ordinal */
   uint32_t buffer_mode;        /* fdas_buffer_mode */
   uint32_t sync_pipeline;      /* FDAS::initialise_accelerator sync_pipeline */
-  uint32_t recheck;            /* 1 = FP64 recheck of near-threshold cells (default) */
+  uint32_t recheck;            /* 1 = FP64-grade recheck of near-threshold cells (default) */
   float recheck_band;          /* relative band around each threshold; 0 = 1e-4 */
   uint32_t overlap;            /* 1 = size the kernels so that the FT convolution of one
                                   buffer set and the harmonic summing of the other run
