@@ -13,11 +13,15 @@ constexpr int kWarpsPerCta = 8;
 // One warp per tile.  Tile i covers spectrum bins [i P - O, i P + P): bins
 // below 0 (the first tile's overlap) and from N on (the last tile's padding)
 // read as zero -- tile_input.cl.mako:42-94 / ft_conv.py:165-180.
+// Three warps per CTA and three CTAs per SM (at most 224 registers): 9 warps
+// per SM, so the 1289 tiles of a 2^21-bin search run in a single wave
+// (1368 warp slots) instead of 1216 + 73.
+constexpr int kTileWarps = 3;
 template <bool BATCH>
-__global__ void __launch_bounds__(256) tile_fft_kernel(TileParams p) {
+__global__ void __launch_bounds__(32 * kTileWarps, 3) tile_fft_kernel(TileParams p) {
   extern __shared__ float4 smem_f4[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile = blockIdx.x * kWarpsPerCta + warp;
+  const int tile = blockIdx.x * kTileWarps + warp;
   if (tile >= p.n_tiles) return;
   float *ex = reinterpret_cast<float *>(smem_f4) + warp * kExFloats;
   const TwiddleBases tb = load_twiddle_bases<-1>(p.twiddle, lane);
@@ -320,12 +324,12 @@ __global__ void taps_kernel(TapsParams p) {
 static int ex_smem_bytes() { return kWarpsPerCta * kExFloats * (int)sizeof(float); }
 
 cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s) {
-  const int smem = ex_smem_bytes();
+  const int smem = kTileWarps * kExFloats * (int)sizeof(float);
   auto kern = p.trials ? tile_fft_kernel<true> : tile_fft_kernel<false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((p.n_tiles + kWarpsPerCta - 1) / kWarpsPerCta);
-  kern<<<grid, 256, smem, s>>>(p);
+  dim3 grid((p.n_tiles + kTileWarps - 1) / kTileWarps);
+  kern<<<grid, 32 * kTileWarps, smem, s>>>(p);
   return cudaGetLastError();
 }
 
