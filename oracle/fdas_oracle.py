@@ -8,7 +8,7 @@ reference's own CPU path for the FT convolution and harmonic summing:
 * ``fdas/src/host/gen_info.h`` (candidate location codec)
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may import it, and only as the checker (or as the timed CPU
+``bench.py`` may import it, and only to check results (or as the timed CPU
 baseline).  The product path (``fdas_gb300``) never calls into it.
 
 Parity is pinned: ``tests/golden/make_golden.py`` runs the unmodified
@@ -264,7 +264,7 @@ def compat_list(loc, pwr, plane, n_planes=8, per_plane=512):
 
     The reference keeps a 64-slot x 8-lane ring per plane (detect.cl.mako:32-115,
     store_cands.cl.mako:21-33), i.e. 512 entries per plane and 4096 in total,
-    overwriting the oldest slots on overflow.  This build uses a deterministic
+    overwriting the oldest slots on overflow.  fdas_gb300 uses a deterministic
     rule instead: per plane, if more than ``per_plane`` hits exist keep the
     strongest (power descending, location ascending on ties); the kept entries
     are listed in location order and the rest of the plane's block is padded
