@@ -58,6 +58,24 @@ def dist_env():
     return ws, rank, local
 
 
+def reduce_max(v, device):
+    """The largest ``v`` over the ranks (one rank: ``v``).  Timings are
+    combined this way: the job ends when its slowest replica ends."""
+    ws, _, _ = dist_env()
+    if ws == 1:
+        return float(v)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, seconds, ws):
+    """Units all replicas processed per second of the slowest one."""
+    return ws * units_per_rank / seconds
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -280,12 +298,7 @@ def run_ours(args):
         return total, lat
 
     def max_over_ranks(v):
-        if ws > 1:
-            import torch.distributed as dist
-            t = torch.tensor([v], device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            return float(t.item())
-        return v
+        return reduce_max(v, f"cuda:{local}")
 
     d_x = torch.from_numpy(x.view(np.float32)).to(f"cuda:{local}")
     # sequential form: one buffer set, one stream; gives the per-search latency
@@ -313,9 +326,9 @@ def run_ours(args):
             "pipelined": (pipe_ms, clocks, q)}
     mode = min(runs, key=lambda k: runs[k][0])
     total_ms = runs[mode][0]
-    value = ws * args.steps / (total_ms / 1e3)
+    value = whole_job_rate(args.steps, total_ms / 1e3, ws)
     clk = runs[mode][1].summary()  # clocks of the reported loop
-    mode_values = {f"value_{k}": ws * args.steps / (v[0] / 1e3) for k, v in runs.items()}
+    mode_values = {f"value_{k}": whole_job_rate(args.steps, v[0] / 1e3, ws) for k, v in runs.items()}
 
     # ---- stage times (separate pass, so the per-launch host syncs do not
     # disturb the throughput number above)
@@ -368,12 +381,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     barrier()
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = ws * e2e_steps / e2e_s
+    e2e_s = reduce_max(e2e_s, f"cuda:{local}")
+    e2e = whole_job_rate(e2e_steps, e2e_s, ws)
 
     if rank != 0:
         return
