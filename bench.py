@@ -139,48 +139,38 @@ def measured_peaks():
 
 
 # ------------------------------------------------------------------ CPU side
-_WORKER = {}
-
-
-def cpu_worker_init(x, bank, dtype):
-    """Pool initializer: the spectrum and bank are sent to each worker once."""
-    _WORKER.update(x=x, bank=bank, dtype=dtype)
-
-
-def cpu_fop_rows(rows):
-    """FOP rows by direct convolution (ft_conv.py:199-205 semantics)."""
+def cpu_search(x, bank, thr, ex, workers):
+    """One whole CPU search of the reference's path at its own precision:
+    the FOP of all 85 rows by direct linear convolution in complex64
+    (ft_conv.py:199-205: scipy.signal.convolve with the non-zero taps) and
+    harmonic summing of all bins, rows and planes in float32 with the
+    reference's index math and strict '>' (hsum.py:95-151, vectorised).  FOP
+    rows and harmonic-summing bin ranges are spread over the ``workers``
+    threads of the pool ``ex`` (SciPy's FFTs and NumPy's loops release the
+    GIL).  Returns (seconds, candidates)."""
     from oracle import fdas_oracle as O
-    O.fop(_WORKER["x"], _WORKER["bank"], dtype=_WORKER["dtype"], rows=rows)
-    return len(rows)
+    n = x.size
+    fop = np.empty((N_TEMPLATES, n), dtype=np.float32)
 
+    def rows(rs):
+        fop[rs] = O.fop(x, bank, dtype=np.float32, rows=rs)
 
-def cpu_search_time(x, bank, thr, n_rows_sample, bin_frac, dtype, pool=None, workers=1):
-    """Extrapolated time of one CPU search from a bounded sample.
+    def hsum(b):
+        return O.detections_streaming(fop, thr, N_PLANES, dtype=np.float32, bins=b)[0]
 
-    FOP: ``n_rows_sample`` of the 85 rows by direct linear convolution (scaled
-    by 85 / n_rows_sample).  Harmonic summing: the vectorised restatement of
-    hsum.py over the first ``bin_frac`` of the bins for all rows (scaled by
-    1 / bin_frac).  Returns (seconds per search, description).
-    """
-    from oracle import fdas_oracle as O
-    rows = np.linspace(0, N_TEMPLATES - 1, n_rows_sample).astype(int)
     t0 = time.perf_counter()
-    if pool is not None:
-        chunks = np.array_split(rows, workers)
-        pool.map(cpu_fop_rows, [list(c) for c in chunks if len(c)])
-    else:
-        O.fop(x, bank, dtype=dtype, rows=rows)
-    t_fop = (time.perf_counter() - t0) * N_TEMPLATES / n_rows_sample
-    nb = int(x.size * bin_frac)
-    rng = np.random.default_rng(0)
-    plane = rng.exponential(size=(N_TEMPLATES, nb)).astype(dtype)
-    t0 = time.perf_counter()
-    O.detections_streaming(plane, thr, N_PLANES, dtype=dtype)
-    t_hs = (time.perf_counter() - t0) / bin_frac
-    desc = (f"FOP of {n_rows_sample}/85 rows at 2^21 bins (x{N_TEMPLATES / n_rows_sample:.1f}) + vectorised "
-            f"harmonic summing over {nb} of 2^21 bins, 85 rows, 8 planes (x{1 / bin_frac:.0f}); "
-            f"{np.dtype(dtype).name}")
-    return t_fop + t_hs, desc
+    list(ex.map(rows, [list(c) for c in np.array_split(np.arange(N_TEMPLATES), workers) if len(c)]))
+    edges = np.linspace(0, n, 4 * workers + 1).astype(np.int64)
+    locs = list(ex.map(hsum, list(zip(edges[:-1], edges[1:]))))
+    n_cand = int(sum(v.size for v in locs))
+    return time.perf_counter() - t0, n_cand
+
+
+CPU_SAMPLE = ("whole search, nothing sampled or extrapolated: FOP of all 85 rows x 2^21 bins by direct "
+              "linear convolution in complex64 (scipy.signal.convolve, ft_conv.py:199-205) + harmonic summing "
+              "of all 85 rows x 2^21 bins x 8 planes in float32 (hsum.py:95-151 vectorised), the reference's "
+              "CPU path at its own precision, rows and bin ranges spread over {w} host threads; "
+              "{c} candidates per search")
 
 
 def fp32_pipe(ftc_ms, n_bins, clocks):
@@ -212,26 +202,23 @@ def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
+    from concurrent.futures import ThreadPoolExecutor
     x, bank, thr = make_inputs()
     workers = os.cpu_count() or 1
     times = []
-    desc = ""
-    import multiprocessing as mp
-    # one row per worker and 1/64 of the bins per step keeps a step near half
-    # a second on 16 cores, so --steps K --warmup W ends within minutes
-    with mp.get_context("spawn").Pool(workers, initializer=cpu_worker_init, initargs=(x, bank, np.float32)) as pool:
+    with ThreadPoolExecutor(workers) as ex:
         for i in range(args.warmup + args.steps):
-            t, desc = cpu_search_time(x, bank, thr, n_rows_sample=min(N_TEMPLATES, workers), bin_frac=1 / 64,
-                                      dtype=np.float32, pool=pool, workers=workers)
+            t, n_cand = cpu_search(x, bank, thr, ex, workers)
             if i >= args.warmup:
                 times.append(t)
-    v = 1.0 / float(np.mean(times))
+    ms = 1e3 * float(np.mean(times))
+    v = 1e3 / ms
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": WORKLOAD,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(WORKLOAD, parallelism="replicas1"),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
-                             "sample": "per step: " + desc + " (the reference's ft_conv.py + hsum.py path, "
-                                       "restated in NumPy/SciPy at its own float32/complex64 precision)"},
+                             "sample": "one step = one " + CPU_SAMPLE.format(w=workers, c=n_cand)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -388,17 +375,30 @@ def run_ours(args):
         return
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        t_cpu, desc = cpu_search_time(x, bank, thr, n_rows_sample=4, bin_frac=1 / 32, dtype=np.float32)
-        cpu = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "one search extrapolated from: " + desc}
+        from concurrent.futures import ThreadPoolExecutor
+        workers = os.cpu_count() or 1
+        with ThreadPoolExecutor(workers) as ex:
+            t_cpu, n_cpu = cpu_search(x, bank, thr, ex, workers)
+        cpu = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": workers, "kind": "port",
+               "sample": "one " + CPU_SAMPLE.format(w=workers, c=n_cpu)}
     # tiling, FT convolution, harmonic summing, FP64 recheck, 3 selection kernels
     launches_per_search = 7
+    forms = None
+    if ws == 1 and not args.no_forms:
+        # the three forms of the search beside the plain path, short runs of
+        # their own workloads (each reports the plain path it is compared with)
+        p.close()
+        q.close()
+        forms = {"batched": batched_form(256, steps=3, warmup=2),
+                 "served": [served_form(rate, 400, 8) for rate in (400.0, 2000.0)],
+                 "precision": precision_form(N_BINS, steps=20, warmup=3)}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "mode": mode, **mode_values,
         "dtype": "f32", "data": "synthetic", "config": dict(WORKLOAD, parallelism=f"replicas{ws}"),
-        "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
+        "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
+                       "note": "sequential searches one at a time, no load; under load: forms.served"},
         "stage_ms": stage_ms, "candidates": int(n_cand), "candidates_dropped": int(dropped),
         "recheck_cells": counters["recheck"], "device_status": counters["status"],
         "selected_per_plane": counters["selected"],
@@ -415,6 +415,7 @@ def run_ours(args):
         "gpu_launches": launches_per_search * args.steps,
         "clocks": clk,
         "cpu_baseline": cpu,
+        "forms": forms,
     }
     print(json.dumps(line), flush=True)
 
@@ -431,8 +432,8 @@ def served_spectrum(n, seed):
     return synth.spectrum(synth.timeseries(2 * n, sig, seed=seed), n)[0]
 
 
-def run_served(args):
-    """Open request loop: Poisson arrivals at --rate searches/s; each request is
+def served_form(rate, n_req, slots):
+    """Open request loop: Poisson arrivals at ``rate`` searches/s; each request is
     a trial of 2^16..2^22 samples (2^15..2^21 bins), the 85-template bank or
     its z = -21..+21 half, 4, 8 or 16 planes, chi-square FAR 1e-6 thresholds.
     The request server (continuous batching, slots admitted by FOP bytes
@@ -447,6 +448,7 @@ def run_served(args):
     bank = template_bank()
     rng = np.random.default_rng(2025)
     sizes = [1 << k for k in range(15, 22)]
+    args = argparse.Namespace(rate=rate, requests=n_req, slots=slots)
     pool = {n: [served_spectrum(n, 100 * k + i) for i in range(2)] for k, n in enumerate(sizes)}
     thr = {P: np.array([gamma.isf(1e-6, k) for k in range(1, P + 1)], dtype=np.float32) for P in (4, 8, 16)}
     n_req = args.requests
@@ -511,16 +513,17 @@ def run_served(args):
         plain_one(n, half, P, k)
         lat.append((time.perf_counter() - (t0 + ta)) * 1e3)
     plain = stats(lat, time.perf_counter() - t0)
-    line = {"form": "served", "metric": "served searches: p50/p99 latency (submit to candidate list) and searches/s",
+    for h in handles.values():
+        h.close()
+    return {"form": "served", "metric": "served searches: p50/p99 latency (submit to candidate list) and searches/s",
             "unit": "ms", "rate_per_s": args.rate, "requests": n_req, "slots": args.slots,
             "mix": "2^15..2^21 bins (uniform in log2), full 85 or half 43 template bank, 4/8/16 planes, "
                    "0-2 signals, chi-square FAR 1e-6", "served": served, "plain_per_request": plain,
             "data": "synthetic"}
-    print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ batched form
-def run_batched(args):
+def batched_form(n_tr=256, steps=5, warmup=3, autotune=True):
     """256 dedispersed trials of uneven length (log-uniform 2^18..2^22 samples,
     i.e. 2^17..2^21 bins), 0-2 accelerated signals each (z in [-42, 42], 1-8
     harmonics), 85-template bank, 8 planes, chi-square FAR 1e-6: one batched
@@ -533,27 +536,10 @@ def run_batched(args):
     from fdas_gb300.templates import template_bank
     torch.cuda.set_device(0)
     bank = template_bank()
-    rng = np.random.default_rng(4242)
-    n_tr = args.trials
-    n_samp = np.exp(rng.uniform(np.log(2 ** 18), np.log(2 ** 22), n_tr)).astype(np.int64) // 2 * 2
-    n_bins = (n_samp // 2).astype(np.uint32)
+    from fdas_gb300 import synth
+    args = argparse.Namespace(steps=steps, warmup=warmup, no_autotune=not autotune)
     thr = np.array([gamma.isf(1e-6, k) for k in range(1, 9)], dtype=np.float32)
-    # synthetic spectra made on the GPU (input preparation, not timed)
-    g = torch.Generator(device="cuda").manual_seed(7)
-    specs = []
-    for i in range(n_tr):
-        ns = int(n_samp[i])
-        x = torch.randn(ns, device="cuda", generator=g, dtype=torch.float64)
-        u = torch.arange(ns, device="cuda", dtype=torch.float64) / ns
-        for _ in range(int(rng.integers(0, 3))):
-            r0, z, nh = rng.uniform(0.05, 0.45) * ns / 2, rng.uniform(-42, 42), int(rng.integers(1, 9))
-            amp = 0.05 * np.sqrt((1 << 15) / (ns / 2))
-            ph = 2 * np.pi * (r0 * u + 0.5 * z * u * u)
-            for h in range(1, nh + 1):
-                x += amp * torch.cos(h * ph)
-        X = torch.fft.rfft(x.float().double())[: ns // 2] / np.sqrt(ns)
-        specs.append(torch.view_as_real(X.to(torch.complex64)).contiguous())
-    d_all = torch.cat([s.reshape(-1) for s in specs])
+    n_bins, offs, d_all = synth.batch_mix(n_tr)  # synthetic spectra made on the GPU (not timed)
     torch.cuda.synchronize()
     total_bins = int(n_bins.sum())
 
@@ -580,7 +566,6 @@ def run_batched(args):
     h = FDAS(log)
     assert h.initialise_accelerator(int(n_bins.max())), h.last_error
     assert h.upload_templates(bank, FDAS.A), h.last_error
-    offs = np.concatenate([[0], np.cumsum(n_bins.astype(np.int64))])
 
     def plain_pass():
         for i in range(n_tr):
@@ -620,18 +605,19 @@ def run_batched(args):
         plain_alt_pass()
         pa.append(time.perf_counter() - t)
     plain_alt_s = float(np.median(pa))
-    line = {"form": "batched", "metric": "batched searches/s (trials of uneven length)", "unit": "searches/s",
+    h.close()
+    h2.close()
+    return {"form": "batched", "metric": "batched searches/s (trials of uneven length)", "unit": "searches/s",
             "value": n_tr / batched_s, "ms_per_batch": batched_s * 1e3, "trials": n_tr, "total_bins": total_bins,
             "fop_gb": 4 * 85 * total_bins / 1e9, "plain_value": n_tr / plain_s, "plain_ms_per_batch": plain_s * 1e3,
             "speedup_vs_plain": plain_s / batched_s, "plain_alternating_ms_per_batch": plain_alt_s * 1e3,
             "speedup_vs_plain_alternating": plain_alt_s / batched_s, "autotune": info, "setup_s": t_setup,
             "candidates": int(n_cand), "steps": args.steps, "warmup": args.warmup,
             "timing": "host clock around graph replays (each ~100 ms), median", "data": "synthetic (seeded, on GPU)"}
-    print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ precision form
-def run_precision(args):
+def precision_form(bins=N_BINS, steps=50, warmup=3, noise_only=False):
     """The 2^21-bin search with the inverse DFT of the FT convolution on the
     tensor cores (split BF16 / split FP16 operands, tcgen05) beside the FP32 FFT
     path: searches/s, FT-convolution stage time and whether the candidate set
@@ -639,7 +625,8 @@ def run_precision(args):
     import torch
     from fdas_gb300.fdas import FDAS
     torch.cuda.set_device(0)
-    x, bank, thr = make_inputs(args.bins, args.noise_only)
+    args = argparse.Namespace(bins=bins, steps=steps, warmup=warmup)
+    x, bank, thr = make_inputs(bins, noise_only)
     d_x = torch.from_numpy(x.view(np.float32)).cuda()
     log = open(os.devnull, "w")
     out = {}
@@ -672,10 +659,9 @@ def run_precision(args):
         out[name] = {"searches_per_s": 1e3 / ms, "ms_per_search": ms, "ft_convolution_ms": float(st[2]),
                      "candidates": n_total, "same_candidates_as_fp32": keys == ref_keys}
         h.close()
-    line = {"form": "precision", "metric": "searches/s at 2^21 bins x 85 tmpl x 8 harm by inverse-DFT precision",
+    return {"form": "precision", "metric": "searches/s at 2^21 bins x 85 tmpl x 8 harm by inverse-DFT precision",
             "unit": "searches/s", "n_bins": args.bins, "steps": args.steps, "warmup": args.warmup,
             "results": out, "data": "synthetic", "timing": "CUDA events on the library stream, sequential searches"}
-    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -690,6 +676,8 @@ def main():
     ap.add_argument("--stage-times", action="store_true", help="per-step stage events inside the timed loop")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="device-resident leg only (profiling runs)")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="leave out the short batched / served / precision runs of the default line")
     ap.add_argument("--noise-only", action="store_true",
                     help="Gaussian noise without the injected signals (profiling the no-candidate path)")
     ap.add_argument("--bins", type=int, default=N_BINS,
@@ -708,13 +696,13 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     if args.form == "served":
-        run_served(args)
+        print(json.dumps(served_form(args.rate, args.requests, args.slots)), flush=True)
         return
     if args.form == "batched":
-        run_batched(args)
+        print(json.dumps(batched_form(args.trials, args.steps, args.warmup, not args.no_autotune)), flush=True)
         return
     if args.form == "precision":
-        run_precision(args)
+        print(json.dumps(precision_form(args.bins, args.steps, args.warmup, args.noise_only)), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -17,8 +17,14 @@ OK, ERR_INVALID_ARG, ERR_OUT_OF_MEMORY, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED, 
 STATUS_NAMES = ["OK", "INVALID_ARG", "OUT_OF_MEMORY", "CUDA", "TIMEOUT", "UNSUPPORTED", "CAPACITY", "STATE",
                 "NO_DEVICE"]
 
+# fdas_set_fault_injection flags
+INJECT_FTC_STALL = 1
+
 # fdas_template_layout
 TEMPLATES_FFT_P4, TEMPLATES_FFT_NATURAL, TEMPLATES_TIME_DOMAIN = 0, 1, 2
+
+
+LOG_FN = ctypes.CFUNCTYPE(None, ctypes.c_char_p, ctypes.c_void_p)
 
 
 class FdasConfig(ctypes.Structure):
@@ -37,6 +43,9 @@ class FdasConfig(ctypes.Structure):
         ("recheck_band", ctypes.c_float),
         ("overlap", ctypes.c_uint32),
         ("precision", ctypes.c_uint32),
+        ("trace_enqueue", ctypes.c_uint32),
+        ("log_fn", LOG_FN),
+        ("log_user", ctypes.c_void_p),
     ]
 
 
@@ -44,8 +53,6 @@ class FdasCandidate(ctypes.Structure):
     _fields_ = [("harmonic", ctypes.c_uint32), ("template_num", ctypes.c_int32), ("bin", ctypes.c_uint32),
                 ("power", ctypes.c_float)]
 
-
-LOG_FN = ctypes.CFUNCTYPE(None, ctypes.c_char_p, ctypes.c_void_p)
 
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
@@ -74,6 +81,8 @@ SIGNATURES = {
     "fdas_print_stats": (None, [_P, _INT, _INT]),
     "fdas_print_events": (None, [_P, _INT]),
     "fdas_set_log": (None, [_P, LOG_FN, _P]),
+    "fdas_set_wait_timeout": (_INT, [_P, ctypes.c_int64]),
+    "fdas_set_fault_injection": (_INT, [_P, _U32]),
     "fdas_get_stage_times": (_INT, [_P, _INT, _P]),
     "fdas_get_input_sz": (_U32, [_P]),
     "fdas_get_tiles_sz": (_U32, [_P]),

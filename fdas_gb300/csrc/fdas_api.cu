@@ -8,9 +8,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <numeric>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -34,7 +36,9 @@ constexpr int kCtrlSelCount = kCtrlCount + kMaxPlanes;
 constexpr int kCtrlSelLo = kCtrlSelCount + kMaxPlanes;
 constexpr int kCtrlItems = kCtrlSelLo + kMaxPlanes;  // harmonic-summing work counter
 constexpr int kCtrlBound = kCtrlItems + 1;           // + plane: boundary records of the selection
-constexpr int kCtrlWords = kCtrlBound + kMaxPlanes;
+constexpr int kCtrlWords = kCtrlBound + kMaxPlanes;   // zeroed before every harmonic summing
+constexpr int kCtrlFtcStatus = kCtrlWords;           // FT-convolution status, zeroed before each FT convolution
+constexpr int kCtrlStride = kCtrlWords + 1;          // control words per buffer set
 constexpr uint32_t kDefaultCapacity = 1u << 22;     // candidate records per buffer set
 constexpr uint32_t kMaxCapacity = 1u << 27;
 constexpr int kRecheckCap = 65536;
@@ -78,6 +82,7 @@ struct BufferSet {
   uint32_t *p_loc = nullptr;
   float *p_pwr = nullptr;
   bool ev_ftc_recorded = false;
+  bool ftc_unchecked = false;  // an FT convolution ran whose status word has not been checked
 };
 
 }  // namespace
@@ -99,10 +104,16 @@ struct fdas_handle {
   int alloc_N = 0, alloc_T = 0, alloc_P = 0, alloc_tiles = 0;
   size_t alloc_fop_floats = 0;
   BufferSet set[2];
-  // print_stats bookkeeping
-  float pipeline_accum_ms = 0.f;
+  long long wait_timeout_ns = kWaitNs;  // bound on the kernels' waits (fdas_set_wait_timeout)
+  uint32_t inject = 0;                   // fdas_set_fault_injection flags
+  // print_stats / print_events bookkeeping: device event times are placed on
+  // the host's steady clock through an anchor event recorded (and waited for)
+  // at initialisation
+  cudaEvent_t anchor = nullptr;
+  long long anchor_ns = 0;       // steady-clock time of the anchor event
+  long long pipeline_start_ns = 0;
+  long long pipeline_accum_ns = 0;
   unsigned pipeline_launches = 0;
-  cudaEvent_t pipeline_start = nullptr;
 };
 
 namespace {
@@ -138,6 +149,17 @@ fdas_status cuda_fail(fdas_handle *h, cudaError_t e, const char *what, const cha
   } while (0)
 
 bool valid_set(fdas_buffer_set ab) { return ab == FDAS_SET_A || ab == FDAS_SET_B; }
+
+long long steady_ns() {
+  return (long long)std::chrono::duration_cast<std::chrono::nanoseconds>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+long long system_ns() {
+  return (long long)std::chrono::duration_cast<std::chrono::nanoseconds>(
+             std::chrono::system_clock::now().time_since_epoch())
+      .count();
+}
 bool valid_part(fdas_fop_part w) {
   return w == FDAS_NEGATIVE_ACCELERATIONS || w == FDAS_POSITIVE_ACCELERATIONS || w == FDAS_ALL_ACCELERATIONS;
 }
@@ -283,12 +305,18 @@ fdas_status enqueue_ftc(fdas_handle *h, int ab, fdas_fop_part which) {
   p.payload = h->payload;
   rows_of(h, which, &p.row_begin, &p.n_rows);
   p.twiddle = h->d_twiddle;
-  p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlStatus);
-  p.timeout_ns = 2000000000LL;  // 2 s
+  p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlFtcStatus);
+  p.timeout_ns = h->wait_timeout_ns;
   p.ctas_per_sm = h->cfg.overlap ? 1 : 2;
   p.variant = h->cfg.precision == 1 ? 3 : h->cfg.precision == 2 ? 4 : 0;
+  if (h->inject & FDAS_INJECT_FTC_STALL) {
+    p.inject_stall = 1;
+    p.variant = 2;  // the hook lives in the warp-pair FFT kernel
+  }
+  CK(h, cudaMemsetAsync(S.d_ctrl + kCtrlFtcStatus, 0, sizeof(unsigned), S.stream));
   CK(h, launch_ftc(p, S.stream));
   CK(h, cudaEventRecord(S.ev[3], S.stream));
+  S.ftc_unchecked = true;
   S.ev_ftc_recorded = true;
   S.fop_from_input = true;
   return FDAS_OK;
@@ -340,7 +368,7 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   p.rc_count = S.d_ctrl + kCtrlRecheckCount;
   p.rc_cap = h->rc_cap;
   p.status = reinterpret_cast<int *>(S.d_ctrl + kCtrlStatus);
-  p.timeout_ns = 2000000000LL;  // 2 s
+  p.timeout_ns = h->wait_timeout_ns;
 
   if (hsum_smem_bytes(p) > 227 * 1024)
     return fail(h, FDAS_ERR_UNSUPPORTED, "harmonic summing staging exceeds shared memory (too many templates x planes)");
@@ -386,7 +414,7 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   f.invalid_location = (uint32_t)((h->H + 1 + h->H) & 0x7f) << 22;  // encode(1, H+1, 0), gen_info.h:69
   f.status = p.status;
   CK(h, launch_select(f, S.stream));
-  CK(h, cudaMemcpyAsync(S.h_ctrl, S.d_ctrl, sizeof(unsigned) * kCtrlWords, cudaMemcpyDeviceToHost, S.stream));
+  CK(h, cudaMemcpyAsync(S.h_ctrl, S.d_ctrl, sizeof(unsigned) * kCtrlStride, cudaMemcpyDeviceToHost, S.stream));
   CK(h, cudaEventRecord(S.ev[4], S.stream));
   S.ctrl_valid = true;
   return FDAS_OK;
@@ -411,12 +439,26 @@ fdas_status release_pending(fdas_handle *h, int ab) {
   return enqueue_download(h, ab, S.p_loc, S.p_pwr);
 }
 
-fdas_status sync_set(fdas_handle *h, int ab) {
+// Device-side timeouts of the last search on set `ab`, once its stream has
+// completed: the status words come back with the candidate counters; an FT
+// convolution run without harmonic summing has its word read here.
+fdas_status check_timeouts(fdas_handle *h, int ab) {
   BufferSet &S = h->set[ab];
-  CK(h, cudaStreamSynchronize(S.stream));
+  unsigned ftc = 0;
+  if (S.ftc_unchecked) {
+    if (S.ctrl_valid) ftc = S.h_ctrl[kCtrlFtcStatus];
+    else CK(h, cudaMemcpy(&ftc, S.d_ctrl + kCtrlFtcStatus, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  }
+  if (ftc & kStatusFtcTimeout) return fail(h, FDAS_ERR_TIMEOUT, "FT convolution: template staging timed out");
   if (S.ctrl_valid && (S.h_ctrl[kCtrlStatus] & kStatusHsumTimeout))
     return fail(h, FDAS_ERR_TIMEOUT, "harmonic summing: shared-memory staging timed out");
   return FDAS_OK;
+}
+
+fdas_status sync_set(fdas_handle *h, int ab) {
+  BufferSet &S = h->set[ab];
+  CK(h, cudaStreamSynchronize(S.stream));
+  return check_timeouts(h, ab);
 }
 
 float elapsed(cudaEvent_t a, cudaEvent_t b) {
@@ -513,6 +555,11 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice", __FILE__, __LINE__);
 
   fdas_handle *h = new fdas_handle();
+  h->log_fn = cfg.log_fn;
+  h->log_user = cfg.log_user;
+  // FDAS.cpp:60-63: wall-clock and steady-clock times, to map the steady-clock
+  // times of the "%%%" and "@@@" lines onto wall-clock time
+  logf(h, "^^^,%lld,%lld", system_ns(), steady_ns());
   h->cfg = cfg;
   h->cfg.tile_overlap = O;
   h->cfg.candidate_capacity = cap;
@@ -532,6 +579,7 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
 
   auto bail = [&](fdas_status st) {
     g_init_error = h->err;
+    if (h->anchor) cudaEventDestroy(h->anchor);
     for (auto &S : h->set) free_set(S);
     cudaFree(h->d_twiddle);
     cudaFree(h->d_twiddle64);
@@ -578,7 +626,7 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
         {(void **)&S.d_fop, sizeof(float) * fop_floats},
         {(void **)&S.d_key, sizeof(unsigned long long) * (size_t)h->cap},
         {(void **)&S.d_pwr, sizeof(float) * (size_t)h->cap},
-        {(void **)&S.d_ctrl, sizeof(unsigned) * kCtrlWords},
+        {(void **)&S.d_ctrl, sizeof(unsigned) * kCtrlStride},
         {(void **)&S.d_rc, sizeof(uint4) * kRecheckCap},
         {(void **)&S.d_hist, sizeof(unsigned) * (size_t)h->P * kSelBuckets},
         {(void **)&S.d_ticket, sizeof(unsigned)},
@@ -598,14 +646,14 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
     if ((e = cudaMemset(S.d_fop, 0, sizeof(float) * fop_floats)) != cudaSuccess ||
         (e = cudaMemset(S.d_hist, 0, sizeof(unsigned) * (size_t)h->P * kSelBuckets)) != cudaSuccess ||
         (e = cudaMemset(S.d_ticket, 0, sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMemset(S.d_ctrl, 0, sizeof(unsigned) * kCtrlWords)) != cudaSuccess ||
-        (e = cudaHostAlloc((void **)&S.h_ctrl, sizeof(unsigned) * kCtrlWords, cudaHostAllocDefault)) !=
+        (e = cudaMemset(S.d_ctrl, 0, sizeof(unsigned) * kCtrlStride)) != cudaSuccess ||
+        (e = cudaHostAlloc((void **)&S.h_ctrl, sizeof(unsigned) * kCtrlStride, cudaHostAllocDefault)) !=
             cudaSuccess ||
         (e = cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking)) != cudaSuccess) {
       cuda_fail(h, e, "buffer set initialisation", __FILE__, __LINE__);
       return bail(FDAS_ERR_CUDA);
     }
-    std::memset(S.h_ctrl, 0, sizeof(unsigned) * kCtrlWords);
+    std::memset(S.h_ctrl, 0, sizeof(unsigned) * kCtrlStride);
     if (make_hsum_maps(h, S) != FDAS_OK) return bail(FDAS_ERR_CUDA);
     for (auto &ev : S.ev) {
       if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
@@ -614,6 +662,14 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
       }
     }
   }
+  // the anchor placing device events on the host's steady clock
+  if ((e = cudaEventCreate(&h->anchor)) != cudaSuccess ||
+      (e = cudaEventRecord(h->anchor, h->set[0].stream)) != cudaSuccess ||
+      (e = cudaEventSynchronize(h->anchor)) != cudaSuccess) {
+    cuda_fail(h, e, "anchor event", __FILE__, __LINE__);
+    return bail(FDAS_ERR_CUDA);
+  }
+  h->anchor_ns = steady_ns();
   logf(h, "[INFO] Device %d: %d bins, %d templates, %d tiles (overlap %d), %d planes", cfg.device, h->N, h->T,
        h->n_tiles, h->O, h->P);
   *out = h;
@@ -627,7 +683,7 @@ void fdas_destroy(fdas_handle *h) {
   cudaFree(h->d_twiddle);
   cudaFree(h->d_twiddle64);
   cudaFree(h->d_series_tw);
-  if (h->pipeline_start) cudaEventDestroy(h->pipeline_start);
+  if (h->anchor) cudaEventDestroy(h->anchor);
   delete h;
 }
 
@@ -855,9 +911,13 @@ fdas_status fdas_launch(fdas_handle *h, const fdas_complex *input, const float *
   fdas_status st;
   // FDAS.cpp:549-550: launching releases the other set's held-back stage
   if (h->cfg.sync_pipeline && (st = release_pending(h, 1 - ab)) != FDAS_OK) return st;
+  long long t[5];  // steady-clock times around the enqueue steps (FDAS.cpp:556-566)
+  t[0] = steady_ns();
   if ((st = enqueue_input(h, ab, input, false)) != FDAS_OK) return st;
   if ((st = enqueue_tiling(h, ab)) != FDAS_OK) return st;
+  t[1] = steady_ns();
   if ((st = enqueue_ftc(h, ab, which)) != FDAS_OK) return st;
+  t[2] = steady_ns();
   BufferSet &S = h->set[ab];
   if (h->cfg.sync_pipeline) {
     S.pending = true;
@@ -867,10 +927,22 @@ fdas_status fdas_launch(fdas_handle *h, const fdas_complex *input, const float *
     S.p_loc = detection_location;
     S.p_pwr = detection_power;
     S.launched = true;
-    return FDAS_OK;
+    t[3] = t[4] = steady_ns();  // harmonic summing and download are enqueued later
+  } else {
+    if ((st = enqueue_hsum(h, ab, thresholds, which)) != FDAS_OK) return st;
+    t[3] = steady_ns();
+    if ((st = enqueue_download(h, ab, detection_location, detection_power)) != FDAS_OK) return st;
+    t[4] = steady_ns();
   }
-  if ((st = enqueue_hsum(h, ab, thresholds, which)) != FDAS_OK) return st;
-  return enqueue_download(h, ab, detection_location, detection_power);
+  if (h->cfg.trace_enqueue) {
+    // FDAS.cpp:567-575: whole milliseconds of the enqueue steps, then the raw times
+    const char c = ab == FDAS_SET_A ? 'A' : 'B';
+    logf(h, "[INFO] Enqueueing: %c\n       %lldms\n       %lldms\n       %lldms\n       %lldms\n       %lldms", c,
+         (t[4] - t[0]) / 1000000, (t[1] - t[0]) / 1000000, (t[2] - t[1]) / 1000000, (t[3] - t[2]) / 1000000,
+         (t[4] - t[3]) / 1000000);
+    logf(h, "%%%%%%,%c,%lld,%lld,%lld,%lld,%lld,", c, t[0], t[1], t[2], t[3], t[4]);
+  }
+  return FDAS_OK;
 }
 
 fdas_status fdas_enqueue_search_device(fdas_handle *h, const fdas_complex *d_input, const float *thresholds,
@@ -910,9 +982,7 @@ fdas_status fdas_wait(fdas_handle *h, fdas_buffer_set ab) {
   if (!S.launched) return fail(h, FDAS_ERR_STATE, "nothing launched on this buffer set");
   CK(h, cudaSetDevice(h->cfg.device));
   CK(h, cudaEventSynchronize(S.ev[5]));
-  if (S.ctrl_valid && (S.h_ctrl[kCtrlStatus] & kStatusHsumTimeout))
-    return fail(h, FDAS_ERR_TIMEOUT, "harmonic summing: shared-memory staging timed out");
-  return FDAS_OK;
+  return check_timeouts(h, ab);
 }
 
 fdas_status fdas_end_pipeline(fdas_handle *h, fdas_buffer_set ab) {
@@ -1108,49 +1178,74 @@ fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out,
   if (!out && n) return fail(h, FDAS_ERR_INVALID_ARG, "out is NULL");
   CK(h, cudaSetDevice(h->cfg.device));
   CK(h, cudaStreamSynchronize(h->set[ab].stream));
-  unsigned ctrl[kCtrlWords];
+  unsigned ctrl[kCtrlStride];
   CK(h, cudaMemcpy(ctrl, h->set[ab].d_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
+  ctrl[kCtrlStatus] |= ctrl[kCtrlFtcStatus];
   for (uint32_t i = 0; i < n && i < (uint32_t)kCtrlSelLo; ++i) out[i] = ctrl[i];
   return FDAS_OK;
+}
+
+// time of a completed event on the host's steady clock (ns), through the
+// handle's anchor event
+static long long event_ns(const fdas_handle *h, cudaEvent_t e) {
+  return h->anchor_ns + (long long)llround(1e6 * (double)elapsed(h->anchor, e));
 }
 
 void fdas_print_stats(fdas_handle *h, fdas_buffer_set ab, int reset) {
   if (!h || !valid_set(ab)) return;
   BufferSet &S = h->set[ab];
-  if (cudaEventSynchronize(S.ev[5]) != cudaSuccess) {
+  if (!S.launched || cudaEventSynchronize(S.ev[5]) != cudaSuccess) {
     cudaGetLastError();
     return;
   }
-  if (reset || !h->pipeline_start) {
-    if (!h->pipeline_start) cudaEventCreate(&h->pipeline_start);
-    // FDAS.cpp:643-666 measures from the first input transfer of the series
-    cudaEventRecord(h->pipeline_start, S.stream);
-    cudaEventSynchronize(h->pipeline_start);
-    h->pipeline_accum_ms = 0.f;
+  // FDAS.cpp:643-666: the series starts at the input transfer of the launch
+  // printed with `reset`; "complete @" is the end of this launch's candidate
+  // transfer, "II" the increase since the previous print
+  if (reset || !h->pipeline_launches) {
+    h->pipeline_start_ns = event_ns(h, S.ev[0]);
+    h->pipeline_accum_ns = 0;
     h->pipeline_launches = 1;
   } else {
     ++h->pipeline_launches;
   }
+  const long long acc = event_ns(h, S.ev[5]) - h->pipeline_start_ns;
   const char set_c = ab == FDAS_SET_A ? 'A' : 'B';
-  logf(h, "[INFO] Launch  #%u%c complete", h->pipeline_launches, set_c);
+  logf(h, "[INFO] Launch  #%u%c complete @ %.3f ms II ~ %.3f ms", h->pipeline_launches, set_c, acc * 1e-6,
+       (acc - h->pipeline_accum_ns) * 1e-6);
   logf(h, "[INFO]   Preparation duration: %.3f ms", elapsed(S.ev[1], S.ev[2]));
   logf(h, "[INFO]   FT convolution and IFFT duration: %.3f ms", elapsed(S.ev[2], S.ev[3]));
   logf(h, "[INFO]   Harmonic summing duration: %.3f ms", elapsed(S.ev[3], S.ev[4]));
   logf(h, "[INFO]   Total duration: %.3f ms", elapsed(S.ev[0], S.ev[5]));
+  h->pipeline_accum_ns = acc;
 }
 
 void fdas_print_events(fdas_handle *h, fdas_buffer_set ab) {
   if (!h || !valid_set(ab)) return;
   BufferSet &S = h->set[ab];
-  if (cudaEventSynchronize(S.ev[5]) != cudaSuccess) {
+  if (!S.launched || cudaEventSynchronize(S.ev[5]) != cudaSuccess) {
     cudaGetLastError();
     return;
   }
-  // FDAS.cpp:668-686: "@@@" line of stage boundaries, here in microseconds
-  // relative to the input transfer start
-  logf(h, "@@@,%c,0,%.1f,%.1f,%.1f,%.1f,%.1f", ab == FDAS_SET_A ? 'A' : 'B', 1e3f * elapsed(S.ev[0], S.ev[1]),
-       1e3f * elapsed(S.ev[0], S.ev[2]), 1e3f * elapsed(S.ev[0], S.ev[3]), 1e3f * elapsed(S.ev[0], S.ev[4]),
-       1e3f * elapsed(S.ev[0], S.ev[5]));
+  // FDAS.cpp:668-686: start and end of the input transfer, tiling, FT
+  // convolution, harmonic summing and candidate transfer; each stage starts
+  // where the one before it ends on the set's stream
+  long long t[6];
+  for (int i = 0; i < 6; ++i) t[i] = event_ns(h, S.ev[i]);
+  logf(h, "@@@,%c,%lld,%lld,%lld,%lld,%lld,%lld,%lld,%lld,%lld,%lld", ab == FDAS_SET_A ? 'A' : 'B', t[0], t[1], t[1],
+       t[2], t[2], t[3], t[3], t[4], t[4], t[5]);
+}
+
+fdas_status fdas_set_fault_injection(fdas_handle *h, uint32_t flags) {
+  CHECK_HANDLE(h);
+  if (flags & ~(uint32_t)FDAS_INJECT_FTC_STALL) return fail(h, FDAS_ERR_INVALID_ARG, "unknown injection flag");
+  h->inject = flags;
+  return FDAS_OK;
+}
+
+fdas_status fdas_set_wait_timeout(fdas_handle *h, int64_t ns) {
+  CHECK_HANDLE(h);
+  h->wait_timeout_ns = ns > 0 ? (long long)ns : kWaitNs;
+  return FDAS_OK;
 }
 
 void fdas_set_log(fdas_handle *h, fdas_log_fn fn, void *user) {
@@ -1498,7 +1593,7 @@ fdas_status fdas_batch_create(const fdas_batch_config *cfg, const fdas_complex *
   BALLOC(b->d_status, sizeof(int));
   BALLOC(b->d_key, sizeof(unsigned long long) * n * cap);
   BALLOC(b->d_pwr, sizeof(float) * n * cap);
-  BALLOC(b->d_ctrl, sizeof(unsigned) * n * kCtrlWords);
+  BALLOC(b->d_ctrl, sizeof(unsigned) * n * kCtrlStride);
   BALLOC(b->d_rc, sizeof(uint4) * n * kBatchRecheckCap);
   BALLOC(b->d_hist, sizeof(unsigned) * n * P * kSelBuckets);
   BALLOC(b->d_ticket, sizeof(unsigned) * n);
@@ -1512,8 +1607,8 @@ fdas_status fdas_batch_create(const fdas_batch_config *cfg, const fdas_complex *
       (e = cudaMemset(b->d_fop, 0, sizeof(float) * b->fop_floats)) != cudaSuccess ||
       (e = cudaMemset(b->d_hist, 0, sizeof(unsigned) * n * P * kSelBuckets)) != cudaSuccess ||
       (e = cudaMemset(b->d_ticket, 0, sizeof(unsigned) * n)) != cudaSuccess ||
-      (e = cudaMemset(b->d_ctrl, 0, sizeof(unsigned) * n * kCtrlWords)) != cudaSuccess ||
-      (e = cudaHostAlloc((void **)&b->h_ctrl, sizeof(unsigned) * n * kCtrlWords, cudaHostAllocDefault)) != cudaSuccess ||
+      (e = cudaMemset(b->d_ctrl, 0, sizeof(unsigned) * n * kCtrlStride)) != cudaSuccess ||
+      (e = cudaHostAlloc((void **)&b->h_ctrl, sizeof(unsigned) * n * kCtrlStride, cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaHostAlloc((void **)&b->h_status, sizeof(int), cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&b->t0)) != cudaSuccess || (e = cudaEventCreate(&b->t1)) != cudaSuccess) {
@@ -1581,8 +1676,8 @@ fdas_status fdas_batch_create(const fdas_batch_config *cfg, const fdas_complex *
     S.d_fop = b->d_fop + t.fop_offset;
     S.d_key = b->d_key + (size_t)i * cap;
     S.d_pwr = b->d_pwr + (size_t)i * cap;
-    S.d_ctrl = b->d_ctrl + (size_t)i * kCtrlWords;
-    S.h_ctrl = b->h_ctrl + (size_t)i * kCtrlWords;
+    S.d_ctrl = b->d_ctrl + (size_t)i * kCtrlStride;
+    S.h_ctrl = b->h_ctrl + (size_t)i * kCtrlStride;
     S.d_rc = b->d_rc + (size_t)i * kBatchRecheckCap;
     S.d_hist = b->d_hist + (size_t)i * P * kSelBuckets;
     S.d_ticket = b->d_ticket + i;

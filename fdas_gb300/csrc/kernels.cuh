@@ -21,6 +21,14 @@ constexpr int kStatusCandidateOverflow = 4;
 constexpr int kStatusSelectionOverflow = 8;
 constexpr int kStatusFtcTimeout = 16;
 
+// Device-side waits.  kWaitNs is the default bound after which a wait is
+// reported as timed out (FtcParams / HsumParams::timeout_ns may lower it);
+// kDrainNs bounds the wait for a kernel's own copies in flight before it
+// exits after a timeout, so no CTA ends with a copy into its shared memory
+// still pending.
+constexpr long long kWaitNs = 2000000000LL;
+constexpr long long kDrainNs = 2000000000LL;
+
 // Candidate record key: plane << 48 | row << 32 | bin.  Ascending key order is
 // (harmonic, template, bin) -- the order of hsum.py's list.
 __host__ __device__ inline unsigned long long cand_key(int plane, int row, int bin) {
@@ -85,6 +93,8 @@ struct FtcParams {
   const BatchTrial *trials = nullptr;  // batched search: tiles of all trials, FOPs per trial
   int n_trials = 0;
   long long tile_begin = 0;  // batched search: global index of the launch's first tile
+  int inject_stall = 0;      // test hook: each warp pair's first template copy is announced on its
+                             // barrier but not issued, so that wait runs out (nothing is in flight)
 };
 
 // ---- (d) harmonic summing + thresholds + candidate compaction (preload,
@@ -118,6 +128,7 @@ struct HsumParams {
   int *status;
   long long timeout_ns;   // bound on every wait
   int lean;               // 1: 3 stages and <= 80 registers (shares an SM with the FT convolution)
+  int order = 0;          // item order: 0 highest blocks first, 1 octaves interleaved
 };
 
 // 2-D tensor maps of the FOP (rows x stride floats), one box shape per plane
@@ -213,6 +224,10 @@ cudaError_t launch_split_taps(double2 *taps, long long n, cudaStream_t s);
 cudaError_t launch_select(const SelectParams &p, cudaStream_t s);
 cudaError_t launch_spectra(const SpectraParams &p, cudaStream_t s);
 cudaError_t launch_taps(const TapsParams &p, cudaStream_t s);
+
+// SM count of the current device, queried on every call (a process may drive
+// GPUs with different SM counts; the query costs well under a microsecond)
+int current_sm_count();
 
 // shared memory bytes needed by launch_hsum for a given plane geometry
 int hsum_smem_bytes(const HsumParams &p);

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
     });
     if (!mbar_wait(bar, parity, p.timeout_ns)) {
       if (lane == 0) atomicOr(p.status, kStatusFtcTimeout);
-      mbar_wait(bar, parity, p.timeout_ns);  // bounded: let the copy land before exiting
+      mbar_wait(bar, parity, kDrainNs);  // bounded: let the copy land before exiting
       return;
     }
     parity ^= 1u;
@@ -236,8 +236,10 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
   }
   fill_twiddle2(twt, p.twiddle);
   __syncthreads();
-  if (item < n_items && tp == 0)
-    prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + item % p.n_rows) * kTile, bar);
+  if (item < n_items && tp == 0) {
+    if (p.inject_stall) mbar_arrive_expect_tx(bar, kTile * 8);  // test hook: a copy that never comes
+    else prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + item % p.n_rows) * kTile, bar);
+  }
   uint32_t parity = 0;
   const int m = 16 * h + (lane & 15);
   const int g = lane >> 4;
@@ -254,7 +256,8 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
     // the decision to go on is made uniform over the pair
     if (!pair_and(pair, mbar_wait(bar, parity, p.timeout_ns))) {
       if (tp == 0) atomicOr(p.status, kStatusFtcTimeout);
-      mbar_wait(bar, parity, p.timeout_ns);  // bounded: let the copy land before exiting
+      // bounded: let the copy land before exiting (the test hook issued none)
+      if (!p.inject_stall) mbar_wait(bar, parity, kDrainNs);
       return;
     }
     parity ^= 1u;
@@ -321,6 +324,16 @@ __global__ void taps_kernel(TapsParams p) {
   p.taps[(long long)r * p.tap_pitch + q] = make_double2(re / 2048.0, im / 2048.0);
 }
 
+int current_sm_count() {
+  int dev = 0, n_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n_sm <= 0) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n_sm;
+}
+
 static int ex_smem_bytes() { return kWarpsPerCta * kExFloats * (int)sizeof(float); }
 
 cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s) {
@@ -346,16 +359,10 @@ static int ftc_variant() {
 
 cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s) {
   if (p.n_rows <= 0 || p.n_tiles <= 0) return cudaSuccess;
-  static int n_sm = 0;
-  if (!n_sm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-    if (n_sm <= 0) n_sm = 1;
-  }
+  const int n_sm = current_sm_count();
   if ((p.variant == 3 || p.variant == 4) && !p.trials) return launch_ftc_tc(p, p.variant == 4, s);
   const long long items = (long long)p.n_tiles * p.n_rows;
-  if ((p.variant ? p.variant : ftc_variant()) == 1) {
+  if ((p.variant ? p.variant : ftc_variant()) == 1 && !p.inject_stall) {  // the test hook is the pair form's
     const int smem = ex_smem_bytes();
     auto kern = p.trials ? ftc_kernel<true> : ftc_kernel<false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

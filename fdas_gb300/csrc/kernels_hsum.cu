@@ -114,17 +114,33 @@ struct HsItem {
   int f0, sgn, tlo;
 };
 
+// Block of item slot `slot` (nb blocks of 256 bins).  The octaves of the
+// blocks are interleaved so that a block's sub-harmonic regions at planes 2,
+// 4 and 8 (bins f/2, f/4, f/8) are staged at about the time those regions'
+// own items stage them as plane 1, while both are still in L2 (and plane 6
+// of block b reads what plane 3 of block b/2 reads): slot s with o trailing
+// one bits and k = s >> (o + 1) is block ((nb - 1) >> o) - k, the k-th block
+// from the top of octave o, i.e. of ((nb - 1) >> (o + 1), (nb - 1) >> o].
+// Octave o holds ceil(M_o / 2) blocks (M_o = (nb - 1) >> o) and its last slot
+// is below nb - 1, so slots [0, nb - 1) map one to one onto blocks
+// [1, nb); block 0 comes last.  Within an octave blocks go from high to low:
+// a signal's harmonic images cover wider bin ranges at higher bins, so the
+// items that emit most start early and light ones fill the end of the launch.
+__device__ __forceinline__ int hs_block(int slot, int nb) {
+  if (slot >= nb - 1) return 0;
+  const int o = __ffs(~slot) - 1;
+  return ((nb - 1) >> o) - (slot >> (o + 1));
+}
+
 __device__ __forceinline__ HsItem hs_item(const HsumParams &p, int it) {
-  // items enumerate (block, half) over the enabled halves, highest blocks
-  // first: a signal's harmonic images cover wider bin ranges at higher bins
-  // (plane j sums f/k for k <= j), so the items that emit most are handed
-  // out early and the light ones fill the end of the launch
+  // items enumerate (block slot, half) over the enabled halves
   const bool neg = p.tlo[0] <= p.half, pos = p.tlo[1] <= p.half;
   const int nb = (p.n_bins + kHsBins - 1) / kHsBins;
-  int blk, halfsel;
-  if (neg && pos) { blk = it >> 1; halfsel = it & 1; }
-  else { blk = it; halfsel = pos ? 1 : 0; }
-  return HsItem{(nb - 1 - blk) * kHsBins, halfsel ? 1 : -1, p.tlo[halfsel]};
+  int slot, halfsel;
+  if (neg && pos) { slot = it >> 1; halfsel = it & 1; }
+  else { slot = it; halfsel = pos ? 1 : 0; }
+  const int blk = p.order == 1 ? hs_block(slot, nb) : nb - 1 - slot;
+  return HsItem{blk * kHsBins, halfsel ? 1 : -1, p.tlo[halfsel]};
 }
 
 __device__ __forceinline__ int hs_n_items(const HsumParams &p) {
@@ -387,14 +403,34 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
       int cur = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
       int nxt = (int)atomicAdd(p.item_counter, (unsigned)kChunk);
       int used = 0;
+      // per stage: the use whose copies may still be in flight (-1: none).  A
+      // stage's copies have landed once the consumers released it.
+      int pending[kHsStages];
+#pragma unroll
+      for (int q = 0; q < kHsStages; ++q) pending[q] = -1;
       for (int s = 0;; ++s) {
         const int st = s % kHsStages, use = s / kHsStages;
         if (use >= 1 && !mbar_wait_parity(empty + st, (use - 1) & 1, p.timeout_ns)) {
           atomicOr(p.status, kStatusHsumTimeout);
-          item_id[st] = -1;
-          mbar_arrive(full + st);
+          // let every copy in flight land (bounded), so that the stop mark
+          // below arrives on a completed phase and no copy outlives the CTA
+          bool drained = true;
+#pragma unroll
+          for (int q = 0; q < kHsStages; ++q)
+            if (pending[q] >= 0) {
+              drained &= mbar_wait_parity(full + q, pending[q] & 1, kDrainNs);
+              drained &= mbar_wait_parity(full2 + q, pending[q] & 1, kDrainNs);
+              pending[q] = -1;
+            }
+          if (drained) {
+            item_id[st] = -1;
+            mbar_arrive(full + st);
+          }
           break;
         }
+#pragma unroll
+        for (int q = 0; q < kHsStages; ++q)
+          if (q == st) pending[q] = -1;  // released by the consumers: its copies have landed
         if (used == kChunk) {
           cur = nxt;
           used = 0;
@@ -407,6 +443,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           break;
         }
         item_id[st] = it;
+#pragma unroll
+        for (int q = 0; q < kHsStages; ++q)
+          if (q == st) pending[q] = use;
         const HsItem item = hs_item(p, it);
         float *stage = stages + st * p.stage_floats;
         const unsigned bytes1 = (unsigned)(p.bw[1] * p.bh[1]) * 4u;
@@ -421,6 +460,14 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           }
         });
       }
+      // consumers that stopped on a timeout leave stages unconsumed: their
+      // copies land before the CTA ends (returns at once when they have)
+#pragma unroll
+      for (int q = 0; q < kHsStages; ++q)
+        if (pending[q] >= 0) {
+          mbar_wait_parity(full + q, pending[q] & 1, kDrainNs);
+          mbar_wait_parity(full2 + q, pending[q] & 1, kDrainNs);
+        }
     }
   } else {
     // ------------------------------------------------------------ consumers
@@ -872,13 +919,7 @@ static cudaError_t launch_hsum_t(const HsumParams &p, const HsumMaps &m, cudaStr
   cudaError_t e =
       cudaFuncSetAttribute(hsum_kernel<MAXP, NW, STAGES, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  static int n_sm = 0;
-  if (!n_sm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-    if (n_sm <= 0) n_sm = 1;
-  }
+  const int n_sm = current_sm_count();
   const int items = (p.n_bins + kHsBins - 1) / kHsBins * 2;
   hsum_kernel<MAXP, NW, STAGES, MINB><<<items < n_sm ? items : n_sm, 32 * (NW + 1), smem, s>>>(p, m);
   return cudaGetLastError();
@@ -904,18 +945,12 @@ cudaError_t launch_split_taps(double2 *taps, long long n, cudaStream_t s) {
 }
 
 cudaError_t launch_recheck(const RecheckParams &p, cudaStream_t s) {
-  recheck_kernel<<<4 * 152, 32 * 8, 0, s>>>(p);
+  recheck_kernel<<<4 * current_sm_count(), 32 * 8, 0, s>>>(p);
   return cudaGetLastError();
 }
 
 cudaError_t launch_select(const SelectParams &p, cudaStream_t s) {
-  static int n_sm = 0;
-  if (!n_sm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-    if (n_sm <= 0) n_sm = 1;
-  }
+  const int n_sm = current_sm_count();
   const int hsmem = p.n_planes * kSelBuckets * 4;
   cudaError_t e = cudaFuncSetAttribute(select_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, hsmem);
   if (e != cudaSuccess) return e;

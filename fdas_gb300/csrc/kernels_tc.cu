@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
     if (!tc_wait(&bar, phase, p.timeout_ns)) {
       if (tid == 0) atomicOr(p.status, kStatusFtcTimeout);
       stop = 1;
+      tc_wait(&bar, phase, kDrainNs);  // bounded: the MMAs end before tensor memory is freed
     }
     phase ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -304,6 +305,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
     if (!tc_wait(&bar, phase, p.timeout_ns)) {
       if (tid == 0) atomicOr(p.status, kStatusFtcTimeout);
       stop = 1;
+      tc_wait(&bar, phase, kDrainNs);  // bounded: the MMAs end before tensor memory is freed
     }
     phase ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -350,9 +352,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
 
 cudaError_t launch_ftc_tc(const FtcParams &p, bool f16, cudaStream_t s) {
   if (p.n_rows <= 0 || p.n_tiles <= 0) return cudaSuccess;
-  int dev = 0, n_sm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  const int n_sm = current_sm_count();
   const long long groups = ((long long)p.n_tiles * p.n_rows + kTcItems - 1) / kTcItems;
   const int grid = (int)(groups < n_sm ? groups : n_sm);
   auto kern = f16 ? ftc_tc_kernel<true> : ftc_tc_kernel<false>;

@@ -90,9 +90,11 @@ class FDAS:
     def initialise_accelerator(self, input_sz, mode=PerSet, sync_pipeline=False, device=0, n_templates=85,
                                max_template_len=421, tile_overlap=0, n_planes=8, candidate_capacity=0,
                                candidates_per_plane_compat=0, recheck=True, recheck_band=0.0, overlap=False,
-                               precision=0):
+                               precision=0, trace_enqueue=False):
         """FDAS::initialise_accelerator (FDAS.h:44-49).  The bitstream and the
-        OpenCL platform / device selectors become a CUDA device ordinal."""
+        OpenCL platform / device selectors become a CUDA device ordinal.
+        ``trace_enqueue``: log the reference's per-launch "[INFO] Enqueueing" and
+        "%%%" lines (FDAS.cpp:556-575)."""
         cfg = _lib.FdasConfig()
         self._lib.fdas_default_config(ctypes.byref(cfg), int(input_sz))
         cfg.n_templates = n_templates
@@ -108,6 +110,9 @@ class FDAS:
         cfg.recheck_band = float(recheck_band)
         cfg.overlap = int(bool(overlap))
         cfg.precision = int(precision)
+        cfg.trace_enqueue = int(bool(trace_enqueue))
+        cfg.log_fn = self._log_cb  # the "^^^" line of initialisation goes to this log too
+        cfg.log_user = None
         if self._h:
             self._lib.fdas_destroy(self._h)
             self._h = ctypes.c_void_p()
@@ -303,6 +308,15 @@ class FDAS:
         return self._check(self._lib.fdas_enqueue_search_device(self._h, ctypes.c_void_p(int(d_input_ptr)),
                                                                 _ptr(thr), int(which), int(ab)),
                            "enqueue_search_device")
+
+    def set_wait_timeout(self, ns):
+        """Bound (ns) on every wait inside the kernels; <= 0 restores 2 s.  A
+        search that runs into it stops and reports FDAS_ERR_TIMEOUT."""
+        return self._check(self._lib.fdas_set_wait_timeout(self._h, int(ns)), "set_wait_timeout")
+
+    def set_fault_injection(self, flags):
+        """Test hook of the timeout path (``_lib.INJECT_FTC_STALL``; 0 = off)."""
+        return self._check(self._lib.fdas_set_fault_injection(self._h, int(flags)), "set_fault_injection")
 
     def synchronize(self, ab):
         return self._check(self._lib.fdas_synchronize(self._h, int(ab)), "synchronize")

@@ -82,3 +82,33 @@ def small_case(n_freq, seed=1, n_signals=1):
                         n_harm=int(rng.integers(1, 9)),
                         amp=float(rng.uniform(0.1, 0.3))))
     return timeseries(2 * n_freq, sig, seed=seed), sig
+
+
+def batch_mix(n_trials=256, seed=4242, device="cuda"):
+    """The batched workload: ``n_trials`` dedispersed trials of uneven length,
+    samples drawn log-uniformly from 2^18 to 2^22 (2^17 .. 2^21 bins), each
+    with 0-2 accelerated signals (random z in [-42, 42], 1-8 harmonics,
+    amplitude 0.05 sigma x sqrt(2^15 / bins)), unit-power spectra made on the
+    GPU with torch (input preparation only).  Returns (n_bins uint32 array,
+    bin offsets int64 array of n_trials + 1, device float32 tensor holding all
+    spectra back to back as (re, im) pairs)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    n_samp = np.exp(rng.uniform(np.log(2 ** 18), np.log(2 ** 22), n_trials)).astype(np.int64) // 2 * 2
+    n_bins = (n_samp // 2).astype(np.uint32)
+    g = torch.Generator(device=device).manual_seed(7)
+    specs = []
+    for i in range(n_trials):
+        ns = int(n_samp[i])
+        x = torch.randn(ns, device=device, generator=g, dtype=torch.float64)
+        u = torch.arange(ns, device=device, dtype=torch.float64) / ns
+        for _ in range(int(rng.integers(0, 3))):
+            r0, z, nh = rng.uniform(0.05, 0.45) * ns / 2, rng.uniform(-42, 42), int(rng.integers(1, 9))
+            amp = 0.05 * np.sqrt((1 << 15) / (ns / 2))
+            ph = 2 * np.pi * (r0 * u + 0.5 * z * u * u)
+            for h in range(1, nh + 1):
+                x += amp * torch.cos(h * ph)
+        X = torch.fft.rfft(x.float().double())[: ns // 2] / np.sqrt(ns)
+        specs.append(torch.view_as_real(X.to(torch.complex64)).contiguous().reshape(-1))
+    offsets = np.concatenate([[0], np.cumsum(n_bins.astype(np.int64))])
+    return n_bins, offsets, torch.cat(specs)

@@ -41,11 +41,12 @@ class FDAS {
     c.device = device;
     c.buffer_mode = (uint32_t)mode;
     c.sync_pipeline = sync_pipeline ? 1u : 0u;
+    c.log_fn = &FDAS::forward_log;  // from the "^^^" line of initialisation on
+    c.log_user = this;
     fdas_destroy(h);
     h = nullptr;
     fdas_status st = fdas_initialise_accelerator(&c, &h);
     if (st != FDAS_OK) return report(st, "initialise_accelerator");
-    fdas_set_log(h, &FDAS::forward_log, this);
     return true;
   }
 

@@ -82,6 +82,11 @@ typedef enum {
   FDAS_TEMPLATES_TIME_DOMAIN = 2
 } fdas_template_layout;
 
+/* A log sink: receives one line at a time, without the newline.  The
+ * reference writes these lines to the std::ostream given to its constructor
+ * (FDAS.h:42). */
+typedef void (*fdas_log_fn)(const char *line, void *user);
+
 typedef struct {
   uint32_t n_frequency_bins;   /* N, the input size (FDAS::initialise_accelerator input_sz) */
   uint32_t n_templates;        /* odd; 85 in the reference (gen_info.h:27) */
@@ -102,6 +107,17 @@ typedef struct {
                                   CUDA cores (default); 1 / 2 = DFT-64 x DFT-32 factor
                                   products on the tensor cores (tcgen05) with split
                                   (hi + lo) BF16 / FP16 operands, FP32 accumulation */
+  uint32_t trace_enqueue;      /* 1 = fdas_launch logs the reference's per-launch host trace:
+                                  "[INFO] Enqueueing: A" with the enqueue times of its
+                                  stages in ms, and "%%%,A,t0,t1,t2,t3,t4," with the
+                                  steady-clock times (ns) around them (FDAS.cpp:556-575).
+                                  0 (default) = off: at a thousand launches per second the
+                                  log sink would become part of the launch cost */
+  fdas_log_fn log_fn;          /* log sink from initialisation on (NULL = stderr): the
+                                  "^^^" clock-sync line and the "[INFO] Device ..." line
+                                  of fdas_initialise_accelerator go here, like every later
+                                  line of the handle (fdas_set_log changes it) */
+  void *log_user;              /* passed to log_fn */
 } fdas_config;
 
 /* Fill `cfg` with the reference's defaults for `n_frequency_bins` bins. */
@@ -109,7 +125,10 @@ void fdas_default_config(fdas_config *cfg, uint32_t n_frequency_bins);
 
 /* FDAS::FDAS + FDAS::initialise_accelerator (FDAS.h:42-49, FDAS.cpp:54-261).
  * Allocates both buffer sets on `cfg->device`.  On failure *out is NULL and the
- * message is available from fdas_last_error(NULL). */
+ * message is available from fdas_last_error(NULL).  Logs first, like
+ * FDAS.cpp:60-63, the line "^^^,<system clock>,<steady clock>" (both in ns
+ * since their epochs) that lets a log reader map the steady-clock times of
+ * "%%%" and "@@@" lines onto wall-clock time. */
 fdas_status fdas_initialise_accelerator(const fdas_config *cfg, fdas_handle **out);
 
 /* Releases all device resources of the handle. */
@@ -220,14 +239,50 @@ fdas_status fdas_retrieve_candidate_list(fdas_handle *h, fdas_candidate *out, ui
 fdas_status fdas_retrieve_candidates_ring(fdas_handle *h, uint32_t *detection_location, float *detection_power,
                                           fdas_fop_part which, fdas_buffer_set ab);
 
-/* FDAS::print_stats / print_events (FDAS.h:75-77, FDAS.cpp:643-686): write the
- * stage timings of the last launch on `ab` to the log (stderr by default). */
+/* FDAS::print_stats (FDAS.h:75, FDAS.cpp:643-666): after the last launch on
+ * `ab` has completed, logs
+ *   "[INFO] Launch  #<n><A|B> complete @ <X> ms II ~ <Y> ms"
+ * where X is the time from the start of the input transfer of the launch
+ * printed with reset != 0 (the start of the series) to the end of this
+ * launch's candidate transfer, and Y the increase of X since the previous
+ * print_stats, then the durations of preparation (tiling), FT convolution,
+ * harmonic summing and the total, one "[INFO]   <phase> duration: <ms> ms"
+ * line each.  The reference prints whole milliseconds; these lines carry three
+ * decimals (a search here takes well under a millisecond). */
 void fdas_print_stats(fdas_handle *h, fdas_buffer_set ab, int reset);
+/* FDAS::print_events (FDAS.h:77, FDAS.cpp:668-686): logs
+ *   "@@@,<A|B>,<input xfer start>,<input xfer end>,<tiling start>,<tiling end>,
+ *    <FT convolution start>,<FT convolution end>,<harmonic summing start>,
+ *    <harmonic summing end>,<candidate xfer start>,<candidate xfer end>"
+ * for the last launch on `ab`: ten times in ns on the host's steady clock (the
+ * reference gives OpenCL profiling times in ns).  The GPU's events are placed
+ * on that clock through an event recorded and waited for at initialisation;
+ * their spacing is exact to the event resolution (about 0.5 us), their offset
+ * to within the few microseconds of that wait. */
 void fdas_print_events(fdas_handle *h, fdas_buffer_set ab);
 
 /* Redirect the handle's log lines ("[INFO] ...", "@@@,...") to a callback. */
-typedef void (*fdas_log_fn)(const char *line, void *user);
 void fdas_set_log(fdas_handle *h, fdas_log_fn fn, void *user);
+
+/* Bound on every wait inside the kernels (a TMA copy or a tensor-core
+ * product that has not landed), after which the search stops, its status
+ * word gets the timeout bit and fdas_wait / fdas_synchronize return
+ * FDAS_ERR_TIMEOUT.  ns <= 0 restores the default of 2 s.  A kernel that
+ * times out still waits, bounded by 2 s, for its own copies in flight before
+ * it exits, so a short bound only turns slow searches into reported errors:
+ * the handle stays usable (no counterpart in the reference, whose OpenCL
+ * waits have no bound). */
+fdas_status fdas_set_wait_timeout(fdas_handle *h, int64_t ns);
+
+/* Test hook for the timeout path (no counterpart in the reference).  With
+ * FDAS_INJECT_FTC_STALL set, the FT convolution of later searches announces
+ * each warp pair's first template copy on its barrier but never issues it, so
+ * that wait cannot complete and runs out after the bound of
+ * fdas_set_wait_timeout: the search stops with the FT-convolution timeout bit
+ * and fdas_wait returns FDAS_ERR_TIMEOUT.  No memory access is made or left
+ * in flight by the hook; 0 switches it off. */
+#define FDAS_INJECT_FTC_STALL 1u
+fdas_status fdas_set_fault_injection(fdas_handle *h, uint32_t flags);
 
 /* Stage times of the last completed launch on `ab`, in milliseconds:
  * [0] input copy, [1] tiling, [2] FT convolution, [3] harmonic summing,
@@ -303,13 +358,19 @@ fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out,
  *              p4 order of fdas_templates_85_350_ft_p4.npy (FFT_P4) or in
  *              natural order (FFT_NATURAL); TIME_DOMAIN is UNSUPPORTED here
  *  tile_overlap overlap-save overlap O (420 for the 421-tap bank); tiles of
- *              2048 bins advance by 2048 - O
+ *              2048 bins advance by 2048 - O.  The caller must give at least
+ *              the longest template's tap count minus 1: this call receives
+ *              spectra, not taps, so it cannot check it, and a shorter overlap
+ *              wraps the convolution around the tile (wrong FOP values,
+ *              FDAS_OK); the handle path refuses such an overlap
  *  which       FOP rows computed (the other part's rows are left untouched)
  *  d_fop       n_templates x fop_stride floats, device memory, row = template
  *              + n_templates / 2; fop_stride >= n_bins
  *  d_status    NULL, or a device int32 that the caller has set to zero: a
  *              kernel wait that timed out (2 s) ORs 16 into it and leaves the
- *              FOP incomplete
+ *              FOP incomplete.  NULL means no timeout report at all: the call
+ *              has returned FDAS_OK when the work is enqueued, and a timed-out
+ *              wait then leaves an incomplete FOP that nothing flags
  *  stream      cudaStream_t (NULL: the default stream); the call only enqueues
  *
  * Limits: ceil(n_bins / (2048 - O)) <= FDAS_NOALLOC_MAX_TILES (2^19 bins and
@@ -317,9 +378,16 @@ fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out,
  * return FDAS_ERR_CAPACITY before any work is enqueued.  Failures are reported
  * by the status only (no message is stored: storing one would allocate).
  *
- * The first call on a device, with that device current, looks up the scratch
- * address (cudaGetSymbolAddress) and copies the twiddle table into it with a
- * synchronous copy; make that first call before capturing a stream.  All calls
+ * The first call on a device, with that device current, is set-up: it looks
+ * up the scratch address (cudaGetSymbolAddress) and copies the twiddle table
+ * into it with a blocking copy.  With CUDA's default lazy module loading
+ * (CUDA_MODULE_LOADING=LAZY) that first call may also be what loads the
+ * library's device code onto the device, and loading allocates device memory
+ * for the code and for the scratch array itself.  So make the first call on
+ * each device at initialisation -- before the observation starts and before
+ * any stream capture -- or set CUDA_MODULE_LOADING=EAGER so that the module
+ * loads when the CUDA context is created; every later call allocates nothing
+ * and does not block.  All calls
  * on one device share the one scratch area: two calls whose work overlaps on
  * the device (different streams with no ordering between them, or several
  * host threads) race and corrupt each other's FOP.  Order them on one stream.

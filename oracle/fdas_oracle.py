@@ -300,27 +300,31 @@ def search(ft, templates, thresholds, n_planes=8, part='all', dtype=np.float64):
     return plane, hps, detections(hps, thresholds, rows)
 
 
-def detections_streaming(fop_plane, thresholds, n_planes=8, part='all', dtype=np.float64):
+def detections_streaming(fop_plane, thresholds, n_planes=8, part='all', dtype=np.float64, bins=None):
     """Candidates of a whole search without materialising all harmonic planes.
 
     Same semantics as ``harmonic_planes`` + ``detections`` (sequential
     accumulation HP_k = HP_{k-1} + FOP[trunc(t/k)][f//k] in ``dtype``), one
-    plane at a time, for full-size (2^21-bin) checks.
+    plane at a time, for full-size (2^21-bin) checks.  ``bins`` = (b0, b1)
+    restricts the search to those frequency bins (the sums read the whole
+    FOP), so bin ranges can be searched in parallel.
     Returns (location, power, plane, row, bin) sorted by location.
     """
     f = np.asarray(fop_plane).astype(dtype, copy=False)
     n_tmpl, n_freq = f.shape
+    b0, b1 = (0, n_freq) if bins is None else bins
     rows = part_rows(part, n_tmpl)
-    hp = f[rows].copy()
-    freqs = np.arange(n_freq)
+    hp = f[rows, b0:b1].copy()
+    freqs = np.arange(b0, b1)
     out = ([], [], [], [], [])
     for h in range(n_planes):
         k = h + 1
         if k > 1:
-            hp += f[subharmonic_row(rows, k, n_tmpl)][:, freqs // k]
+            hp += f[subharmonic_row(rows, k, n_tmpl)[:, None], (freqs // k)[None, :]]
         ri, fi = np.nonzero(hp > np.asarray(thresholds[h], dtype=dtype))
+        fi = fi + b0
         out[0].append(encode_location(k, rows[ri] - n_tmpl // 2, fi))
-        out[1].append(hp[ri, fi])
+        out[1].append(hp[ri, fi - b0])
         out[2].append(np.full(ri.size, h, dtype=np.int64))
         out[3].append(rows[ri])
         out[4].append(fi)

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from conftest import load_golden
-from gpu_util import make_pipeline
+from gpu_util import make_pipeline, candidates_as_arrays
 from test_gpu_parity import fop_within, FOP_REL_TOL
 from fdas_gb300.fdas import FDAS
 from fdas_gb300.templates import template_bank
@@ -90,7 +90,8 @@ def test_precision_candidates_equal_fp64(precision):
     key = lambda r: list(zip(r["harmonic"].tolist(), r["template_num"].tolist(), r["bin"].tolist()))
     assert len(rec) > 0 and key(rec) == key(rec0)
     loc, pwr = O.detections(O.harmonic_planes(O.fop(x, bank64), dtype=np.float64), thr)[:2]
-    assert len(loc) == len(rec)
+    got, _ = candidates_as_arrays(rec)
+    assert np.array_equal(got, loc)  # the same set of (plane, template, bin) as the FP64 oracle
 
 
 def test_precision_rejected_value():

@@ -122,3 +122,24 @@ def test_noalloc_rejects_beyond_limits(bank_p4):
     assert noalloc_call(lib, d_x.data_ptr(), n, t, d_fop.data_ptr(), n, None) == _lib.OK
     torch.cuda.synchronize()
     assert float(d_fop.abs().max().item()) == 0.0
+
+
+def test_noalloc_natural_order_layout(bank_p4):
+    """Template spectra in natural bin order (FDAS_TEMPLATES_FFT_NATURAL) give
+    the same FOP as the p4-order upload of the handle path."""
+    import torch
+    lib = _lib.load()
+    n = 20_000
+    x = spectrum(n, 4)
+    ref = handle_fop(x, bank_p4)
+    natural = np.ascontiguousarray(O.from_p4(bank_p4).astype(np.complex64))
+    d_x = torch.from_numpy(x.view(np.float32)).cuda()
+    d_t = torch.from_numpy(natural.view(np.float32)).cuda()
+    d_fop = torch.full((85, n), float("nan"), dtype=torch.float32, device="cuda")
+    d_status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    assert noalloc_call(lib, d_x.data_ptr(), n, d_t.data_ptr(), d_fop.data_ptr(), n, d_status.data_ptr(),
+                        layout=FDAS.TemplatesFFTNatural) == _lib.OK
+    torch.cuda.synchronize()
+    assert int(d_status.item()) == 0
+    assert fop_within(d_fop.cpu().numpy(), ref).all()
