@@ -128,7 +128,6 @@ struct HsumParams {
   int *status;
   long long timeout_ns;   // bound on every wait
   int lean;               // 1: 3 stages and <= 80 registers (shares an SM with the FT convolution)
-  int order = 0;          // item order: 0 highest blocks first, 1 octaves interleaved
 };
 
 // 2-D tensor maps of the FOP (rows x stride floats), one box shape per plane

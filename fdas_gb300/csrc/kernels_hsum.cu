@@ -114,33 +114,17 @@ struct HsItem {
   int f0, sgn, tlo;
 };
 
-// Block of item slot `slot` (nb blocks of 256 bins).  The octaves of the
-// blocks are interleaved so that a block's sub-harmonic regions at planes 2,
-// 4 and 8 (bins f/2, f/4, f/8) are staged at about the time those regions'
-// own items stage them as plane 1, while both are still in L2 (and plane 6
-// of block b reads what plane 3 of block b/2 reads): slot s with o trailing
-// one bits and k = s >> (o + 1) is block ((nb - 1) >> o) - k, the k-th block
-// from the top of octave o, i.e. of ((nb - 1) >> (o + 1), (nb - 1) >> o].
-// Octave o holds ceil(M_o / 2) blocks (M_o = (nb - 1) >> o) and its last slot
-// is below nb - 1, so slots [0, nb - 1) map one to one onto blocks
-// [1, nb); block 0 comes last.  Within an octave blocks go from high to low:
-// a signal's harmonic images cover wider bin ranges at higher bins, so the
-// items that emit most start early and light ones fill the end of the launch.
-__device__ __forceinline__ int hs_block(int slot, int nb) {
-  if (slot >= nb - 1) return 0;
-  const int o = __ffs(~slot) - 1;
-  return ((nb - 1) >> o) - (slot >> (o + 1));
-}
-
 __device__ __forceinline__ HsItem hs_item(const HsumParams &p, int it) {
-  // items enumerate (block slot, half) over the enabled halves
+  // items enumerate (block, half) over the enabled halves, highest blocks
+  // first: a signal's harmonic images cover wider bin ranges at higher bins
+  // (plane j sums f/k for k <= j), so the items that emit most are handed
+  // out early and the light ones fill the end of the launch
   const bool neg = p.tlo[0] <= p.half, pos = p.tlo[1] <= p.half;
   const int nb = (p.n_bins + kHsBins - 1) / kHsBins;
-  int slot, halfsel;
-  if (neg && pos) { slot = it >> 1; halfsel = it & 1; }
-  else { slot = it; halfsel = pos ? 1 : 0; }
-  const int blk = p.order == 1 ? hs_block(slot, nb) : nb - 1 - slot;
-  return HsItem{blk * kHsBins, halfsel ? 1 : -1, p.tlo[halfsel]};
+  int blk, halfsel;
+  if (neg && pos) { blk = it >> 1; halfsel = it & 1; }
+  else { blk = it; halfsel = pos ? 1 : 0; }
+  return HsItem{(nb - 1 - blk) * kHsBins, halfsel ? 1 : -1, p.tlo[halfsel]};
 }
 
 __device__ __forceinline__ int hs_n_items(const HsumParams &p) {
