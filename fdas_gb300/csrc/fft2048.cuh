@@ -395,37 +395,42 @@ namespace fdas {
 // the same for all lanes; they then feed their p1 halves to the last DFT8 in
 // swapped order, which multiplies the outputs by (-1)^d2 -- harmless, since
 // only |y|^2 is used.  The result is therefore given as |y|^2 only.
-constexpr int kEx2Pitch = 33;                 // complex values per row of the pair buffer
+// Rows of 34 complex values (272 bytes): 16-byte aligned, so pass 1 writes
+// pairs of values with 16-byte stores (the 8 lanes of a store phase hit banks
+// 4 p mod 32, four wide: no conflicts), and the column reads of pass 2 stay
+// conflict-free (a half-warp reads 16 consecutive values of one row).
+constexpr int kEx2Pitch = 34;                 // complex values per row of the pair buffer
 constexpr int kEx2Floats = 64 * kEx2Pitch * 2;  // floats per warp pair (>= 2048 complex)
 
-// Twiddles w^(m p) of the two-warp transform, m < 32, p < 64, stored at
-// [64 m + p] (16 KB of shared memory per CTA, shared by its warp pairs).
+// Twiddles w^(m p) of the two-warp transform, m < 32, p < 64, with the pair
+// (m, m + 1), m even, of each p next to each other: w^(m p) at
+// [128 (m / 2) + 2 p + (m & 1)], so a thread loads two with one 16-byte load
+// (16 KB of shared memory per CTA, shared by its warp pairs).
 constexpr int kTw2Floats = 2 * 32 * 64;
 
 __device__ __forceinline__ void fill_twiddle2(float2 *twt, const float2 *__restrict__ table) {
   for (int i = threadIdx.x; i < 32 * 64; i += blockDim.x) {
     const int m = i >> 6, p = i & 63;
-    twt[i] = __ldg(table + ((m * p) & 2047));
+    twt[128 * (m >> 1) + 2 * p + (m & 1)] = __ldg(table + ((m * p) & 2047));
   }
 }
 
 // Pass 1 + twiddle + write to the pair buffer.  v[a] holds Y[64 a + p] on entry.
 __device__ __forceinline__ void ifft2_pass1(float2 *v, const float2 *twt, float2 *buf, int p) {
   dft32<+1, 0>(v);
-  // V_p[m] = Z_p[m] w^(m p), m = k1 + 4 k2 sits in v[8 k1 + k2]
-  sfor<4>([&](auto K1) {
-    constexpr int k1 = decltype(K1)::value;
-    sfor<8>([&](auto K2) {
-      constexpr int k2 = decltype(K2)::value;
-      constexpr int idx = 8 * k1 + k2;
-      constexpr int m = k1 + 4 * k2;
-      if constexpr (m != 0) v[idx] = cmul(v[idx], twt[64 * m + p]);
-    });
+  // V_p[m] = Z_p[m] w^(m p); Z_p[m] sits in v[pos32(m)]; twiddles two at a time
+  const float4 *tw4 = reinterpret_cast<const float4 *>(twt) + p;
+  sfor<16>([&](auto M2) {
+    constexpr int m = 2 * decltype(M2)::value;
+    const float4 w = tw4[64 * (m >> 1)];
+    if constexpr (m != 0) v[pos32(m)] = cmul(v[pos32(m)], make_float2(w.x, w.y));
+    v[pos32(m + 1)] = cmul(v[pos32(m + 1)], make_float2(w.z, w.w));
   });
-  float2 *row = buf + kEx2Pitch * p;
-  sfor<32>([&](auto M) {
-    constexpr int m = decltype(M)::value;
-    row[m] = v[pos32(m)];
+  float4 *row = reinterpret_cast<float4 *>(buf + kEx2Pitch * p);
+  sfor<16>([&](auto M2) {
+    constexpr int m = 2 * decltype(M2)::value;
+    const float2 a = v[pos32(m)], b = v[pos32(m + 1)];
+    row[m >> 1] = make_float4(a.x, a.y, b.x, b.y);
   });
 }
 
