@@ -618,9 +618,9 @@ def batched_form(n_tr=256, steps=5, warmup=3, autotune=True):
 
 # ------------------------------------------------------------------ precision form
 def precision_form(bins=N_BINS, steps=50, warmup=3, noise_only=False):
-    """The 2^21-bin search with the inverse DFT of the FT convolution on the
-    tensor cores (split BF16 / split FP16 operands, tcgen05) beside the FP32 FFT
-    path: searches/s, FT-convolution stage time and whether the candidate set
+    """The 2^21-bin search with the forward DFT of the tiles and the inverse
+    DFT of the FT convolution on the tensor cores (split BF16 / split FP16
+    operands, tcgen05) beside the FP32 FFT path: searches/s, FT-convolution stage time and whether the candidate set
     equals the FP32 path's (errors against FP64 are measured by the tests)."""
     import torch
     from fdas_gb300.fdas import FDAS
@@ -659,7 +659,7 @@ def precision_form(bins=N_BINS, steps=50, warmup=3, noise_only=False):
         out[name] = {"searches_per_s": 1e3 / ms, "ms_per_search": ms, "ft_convolution_ms": float(st[2]),
                      "candidates": n_total, "same_candidates_as_fp32": keys == ref_keys}
         h.close()
-    return {"form": "precision", "metric": "searches/s at 2^21 bins x 85 tmpl x 8 harm by inverse-DFT precision",
+    return {"form": "precision", "metric": "searches/s at 2^21 bins x 85 tmpl x 8 harm by DFT precision",
             "unit": "searches/s", "n_bins": args.bins, "steps": args.steps, "warmup": args.warmup,
             "results": out, "data": "synthetic", "timing": "CUDA events on the library stream, sequential searches"}
 

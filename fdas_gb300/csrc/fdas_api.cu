@@ -38,7 +38,8 @@ constexpr int kCtrlItems = kCtrlSelLo + kMaxPlanes;  // harmonic-summing work co
 constexpr int kCtrlBound = kCtrlItems + 1;           // + plane: boundary records of the selection
 constexpr int kCtrlWords = kCtrlBound + kMaxPlanes;   // zeroed before every harmonic summing
 constexpr int kCtrlFtcStatus = kCtrlWords;           // FT-convolution status, zeroed before each FT convolution
-constexpr int kCtrlStride = kCtrlWords + 1;          // control words per buffer set
+constexpr int kCtrlTileStatus = kCtrlWords + 1;      // tiling status (tensor-core form), zeroed before each tiling
+constexpr int kCtrlStride = kCtrlWords + 2;          // control words per buffer set
 constexpr uint32_t kDefaultCapacity = 1u << 22;     // candidate records per buffer set
 constexpr uint32_t kMaxCapacity = 1u << 27;
 constexpr int kRecheckCap = 65536;
@@ -83,6 +84,7 @@ struct BufferSet {
   float *p_pwr = nullptr;
   bool ev_ftc_recorded = false;
   bool ftc_unchecked = false;  // an FT convolution ran whose status word has not been checked
+  bool tile_unchecked = false; // a tensor-core tiling ran whose status word has not been checked
 };
 
 }  // namespace
@@ -285,7 +287,15 @@ fdas_status enqueue_tiling(fdas_handle *h, int ab) {
   p.payload = h->payload;
   p.tiles = S.d_tiles;
   p.twiddle = h->d_twiddle;
-  CK(h, launch_tile_fft(p, S.stream));
+  S.ctrl_valid = false;  // the host copy of the control words predates this stage
+  if (h->cfg.precision) {  // precision form: the forward DFT on the tensor cores too
+    CK(h, cudaMemsetAsync(S.d_ctrl + kCtrlTileStatus, 0, sizeof(unsigned), S.stream));
+    CK(h, launch_tile_tc(p, h->cfg.precision == 2, reinterpret_cast<int *>(S.d_ctrl + kCtrlTileStatus),
+                         h->wait_timeout_ns, S.stream));
+    S.tile_unchecked = true;
+  } else {
+    CK(h, launch_tile_fft(p, S.stream));
+  }
   CK(h, cudaEventRecord(S.ev[2], S.stream));
   return FDAS_OK;
 }
@@ -313,6 +323,7 @@ fdas_status enqueue_ftc(fdas_handle *h, int ab, fdas_fop_part which) {
     p.inject_stall = 1;
     p.variant = 2;  // the hook lives in the warp-pair FFT kernel
   }
+  S.ctrl_valid = false;  // the host copy of the control words predates this stage
   CK(h, cudaMemsetAsync(S.d_ctrl + kCtrlFtcStatus, 0, sizeof(unsigned), S.stream));
   CK(h, launch_ftc(p, S.stream));
   CK(h, cudaEventRecord(S.ev[3], S.stream));
@@ -444,12 +455,17 @@ fdas_status release_pending(fdas_handle *h, int ab) {
 // convolution run without harmonic summing has its word read here.
 fdas_status check_timeouts(fdas_handle *h, int ab) {
   BufferSet &S = h->set[ab];
-  unsigned ftc = 0;
-  if (S.ftc_unchecked) {
-    if (S.ctrl_valid) ftc = S.h_ctrl[kCtrlFtcStatus];
-    else CK(h, cudaMemcpy(&ftc, S.d_ctrl + kCtrlFtcStatus, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  unsigned word[2] = {0u, 0u};  // FT convolution, tiling
+  if (S.ftc_unchecked || S.tile_unchecked) {
+    if (S.ctrl_valid) {
+      word[0] = S.h_ctrl[kCtrlFtcStatus];
+      word[1] = S.h_ctrl[kCtrlTileStatus];
+    } else {
+      CK(h, cudaMemcpy(word, S.d_ctrl + kCtrlFtcStatus, sizeof(word), cudaMemcpyDeviceToHost));
+    }
   }
-  if (ftc & kStatusFtcTimeout) return fail(h, FDAS_ERR_TIMEOUT, "FT convolution: template staging timed out");
+  if (word[1] & kStatusFtcTimeout) return fail(h, FDAS_ERR_TIMEOUT, "tiling: tensor-core wait timed out");
+  if (word[0] & kStatusFtcTimeout) return fail(h, FDAS_ERR_TIMEOUT, "FT convolution: template staging timed out");
   if (S.ctrl_valid && (S.h_ctrl[kCtrlStatus] & kStatusHsumTimeout))
     return fail(h, FDAS_ERR_TIMEOUT, "harmonic summing: shared-memory staging timed out");
   return FDAS_OK;
@@ -1180,7 +1196,7 @@ fdas_status fdas_get_counters(fdas_handle *h, fdas_buffer_set ab, uint32_t *out,
   CK(h, cudaStreamSynchronize(h->set[ab].stream));
   unsigned ctrl[kCtrlStride];
   CK(h, cudaMemcpy(ctrl, h->set[ab].d_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost));
-  ctrl[kCtrlStatus] |= ctrl[kCtrlFtcStatus];
+  ctrl[kCtrlStatus] |= ctrl[kCtrlFtcStatus] | ctrl[kCtrlTileStatus];
   for (uint32_t i = 0; i < n && i < (uint32_t)kCtrlSelLo; ++i) out[i] = ctrl[i];
   return FDAS_OK;
 }

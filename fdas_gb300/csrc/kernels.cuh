@@ -95,6 +95,11 @@ struct FtcParams {
   long long tile_begin = 0;  // batched search: global index of the launch's first tile
   int inject_stall = 0;      // test hook: each warp pair's first template copy is announced on its
                              // barrier but not issued, so that wait runs out (nothing is in flight)
+  // forward transform of the tiles on the tensor cores (precision form):
+  // items are tiles, read from `input` (n_bins spectrum values) and written
+  // to `tiles_out` as complex spectra
+  const float2 *input = nullptr;
+  float2 *tiles_out = nullptr;
 };
 
 // ---- (d) harmonic summing + thresholds + candidate compaction (preload,
@@ -215,6 +220,9 @@ cudaError_t launch_tile_fft(const TileParams &p, cudaStream_t s);
 cudaError_t launch_ftc(const FtcParams &p, cudaStream_t s);
 // precision form: inverse DFT on tcgen05 with split FP16 (f16) or BF16 operands
 cudaError_t launch_ftc_tc(const FtcParams &p, bool f16, cudaStream_t s);
+// precision form: tiling + forward DFT of the tiles on tcgen05, the same DFT
+// factors conjugated; status / timeout as for the FT convolution
+cudaError_t launch_tile_tc(const TileParams &p, bool f16, int *status, long long timeout_ns, cudaStream_t s);
 cudaError_t launch_hsum(const HsumParams &p, const HsumMaps &m, cudaStream_t s);
 // consumer warps of the harmonic-summing kernel for `half` (4 templates each)
 int hsum_warps(int half);

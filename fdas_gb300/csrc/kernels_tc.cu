@@ -1,7 +1,8 @@
-// Precision form of the FT convolution: the inverse 2048-point DFT of every
-// (tile, template) item as two DFT-factor matrix products on the 5th-generation
-// tensor cores (tcgen05.mma, accumulators in tensor memory), with split
-// (hi + lo) BF16 or FP16 operands and FP32 accumulation.
+// Precision form: the 2048-point DFTs of the search as two DFT-factor matrix
+// products on the 5th-generation tensor cores (tcgen05.mma, accumulators in
+// tensor memory), with split (hi + lo) BF16 or FP16 operands and FP32
+// accumulation -- the inverse DFT of every (tile, template) item of the FT
+// convolution, and (FWD) the forward DFT of every tile.
 //
 // With k = 32 k1 + k2 and n = n1 + 64 n2 (k1, n1 < 64; k2, n2 < 32):
 //   y[n1 + 64 n2] = sum_k2 W32^(n2 k2) w^(n1 k2) sum_k1 W64^(n1 k1) Y[32 k1 + k2]
@@ -13,7 +14,9 @@
 // Each product is hi*hi + hi*lo + lo*hi of the split operands (the lo*lo term,
 // 2^-16 of the product for BF16, is dropped).  The operands are scaled by a
 // power of two per group (FP16 range) and the power |y|^2 is scaled back
-// exactly.  The forward transform of the tiles stays on the FP32 path.
+// exactly.  The forward transform (FWD) is the same with the conjugate
+// factors (w = e^(-2 pi i / 2048)): Y is the tile's input (spectrum bins
+// [i P - O, i P + P), zero outside [0, N)), y its spectrum, stored complex.
 //
 // Operands live in shared memory in the tensor core's canonical K-major layout
 // without swizzle: 8 x 16-byte core matrices, K-adjacent ones 128 bytes apart,
@@ -128,7 +131,7 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, long lon
   }
 }
 
-template <bool F16>
+template <bool F16, bool FWD>
 __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
   extern __shared__ __align__(1024) uint8_t tsm[];
   __shared__ __align__(8) uint64_t bar;
@@ -147,7 +150,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       const int kk = kp + u, pin = kk >> 6, k1 = kk & 63;
-      const float2 w = __ldg(p.twiddle + ((32 * n1 * k1) & 2047));
+      float2 w = __ldg(p.twiddle + ((32 * n1 * k1) & 2047));
+      if (FWD) w.y = -w.y;
       v[u] = part == 0 ? (pin == 0 ? w.x : -w.y) : (pin == 0 ? w.y : w.x);
     }
     store_pair<F16>(AAh, AAl, kmaj(m, kp, 128), v[0], v[1]);
@@ -159,13 +163,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       const int kk = kp + u, pin = kk >> 5, k2 = kk & 31;
-      const float2 w = __ldg(p.twiddle + ((64 * n2 * k2) & 2047));
+      float2 w = __ldg(p.twiddle + ((64 * n2 * k2) & 2047));
+      if (FWD) w.y = -w.y;
       v[u] = pout == 0 ? (pin == 0 ? w.x : -w.y) : (pin == 0 ? w.y : w.x);
     }
     store_pair<F16>(BBh, BBl, kmaj(r, kp, 64), v[0], v[1]);
   }
   float2 *TW = reinterpret_cast<float2 *>(tsm + kTW);
-  for (int i = tid; i < 64 * 32; i += kTcThreads) TW[i] = __ldg(p.twiddle + (i & 63) * (i >> 6));
+  for (int i = tid; i < 64 * 32; i += kTcThreads) {
+    float2 w = __ldg(p.twiddle + (i & 63) * (i >> 6));
+    if (FWD) w.y = -w.y;
+    TW[i] = w;
+  }
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&bar)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -183,7 +192,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
   const uint32_t tmem = tmem_slot;
   const int q = warp & 3, h = warp >> 2;  // TMEM lane quadrant, column half
   const uint32_t lane_addr = (uint32_t)(32 * q) << 16;
-  const int n_items = p.n_tiles * p.n_rows;
+  const int n_items = FWD ? p.n_tiles : p.n_tiles * p.n_rows;
   const int n_groups = (n_items + kTcItems - 1) / kTcItems;
   uint32_t phase = 0;
 
@@ -201,12 +210,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
       // loads are unconditional (a missing item reads item 0 and is zeroed), so
       // all 64 of a thread's loads are in flight together
       const int it = g * kTcItems + item, itc = it < n_items ? it : 0;
-      const int tile = itc / p.n_rows, row = p.row_begin + (itc - tile * p.n_rows);
-      const float2 *S = p.tiles + (long long)tile * kTile, *T = p.tmpl + (long long)row * kTile;
       const int k = 32 * k1 + k2;
-      const float2 s0 = __ldg(S + k), t0 = __ldg(T + k), s1 = __ldg(S + k + 32), t1 = __ldg(T + k + 32);
-      float4 v = make_float4(s0.x * t0.x - s0.y * t0.y, s0.x * t0.y + s0.y * t0.x, s1.x * t1.x - s1.y * t1.y,
-                             s1.x * t1.y + s1.y * t1.x);
+      float4 v;
+      if constexpr (FWD) {  // the tile's input bins (tile_input.cl.mako:42-94 / ft_conv.py:165-180)
+        const long long b = (long long)itc * p.payload - p.overlap + k;
+        const float2 zero = make_float2(0.f, 0.f);
+        const float2 x0 = (b >= 0 && b < p.n_bins) ? __ldg(p.input + b) : zero;
+        const float2 x1 = (b + 32 >= 0 && b + 32 < p.n_bins) ? __ldg(p.input + b + 32) : zero;
+        v = make_float4(x0.x, x0.y, x1.x, x1.y);
+      } else {
+        const int tile = itc / p.n_rows, row = p.row_begin + (itc - tile * p.n_rows);
+        const float2 *S = p.tiles + (long long)tile * kTile, *T = p.tmpl + (long long)row * kTile;
+        const float2 s0 = __ldg(S + k), t0 = __ldg(T + k), s1 = __ldg(S + k + 32), t1 = __ldg(T + k + 32);
+        v = make_float4(s0.x * t0.x - s0.y * t0.y, s0.x * t0.y + s0.y * t0.x, s1.x * t1.x - s1.y * t1.y,
+                        s1.x * t1.y + s1.y * t1.x);
+      }
       if (it >= n_items) v = make_float4(0.f, 0.f, 0.f, 0.f);
       y[j] = v;
       mx = fmaxf(mx, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
@@ -325,7 +343,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) ftc_tc_kernel(FtcParams p) {
         for (int jj = 0; jj < 32; ++jj) y[32 * c + jj] += cm[jj];
       }
       const float *yr = y, *yi = y + 32;
-      if (it < n_items) {
+      if (FWD && it < n_items) {  // the tile's spectrum, natural order, unnormalised like fft2048_core
+        float2 *out = p.tiles_out + (long long)it * kTile + n1;
+        const float fs = pow2f(6 - sigma);
+#pragma unroll
+        for (int n2 = 0; n2 < 32; ++n2) out[64 * n2] = make_float2(yr[n2] * fs, yi[n2] * fs);
+      } else if (!FWD && it < n_items) {
         const int tile = it / p.n_rows, row = p.row_begin + (it - tile * p.n_rows);
         float *out = p.fop + (long long)row * p.fop_stride;
         const long long base = (long long)tile * p.payload - p.overlap;
@@ -355,7 +378,30 @@ cudaError_t launch_ftc_tc(const FtcParams &p, bool f16, cudaStream_t s) {
   const int n_sm = current_sm_count();
   const long long groups = ((long long)p.n_tiles * p.n_rows + kTcItems - 1) / kTcItems;
   const int grid = (int)(groups < n_sm ? groups : n_sm);
-  auto kern = f16 ? ftc_tc_kernel<true> : ftc_tc_kernel<false>;
+  auto kern = f16 ? ftc_tc_kernel<true, false> : ftc_tc_kernel<false, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, kTcThreads, kTcSmem, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_tc(const TileParams &t, bool f16, int *status, long long timeout_ns, cudaStream_t s) {
+  if (t.n_tiles <= 0) return cudaSuccess;
+  FtcParams p{};
+  p.input = t.input;
+  p.tiles_out = t.tiles;
+  p.n_bins = t.n_bins;
+  p.n_tiles = t.n_tiles;
+  p.overlap = t.overlap;
+  p.payload = t.payload;
+  p.n_rows = 1;
+  p.twiddle = t.twiddle;
+  p.status = status;
+  p.timeout_ns = timeout_ns;
+  const int n_sm = current_sm_count();
+  const long long groups = ((long long)t.n_tiles + kTcItems - 1) / kTcItems;
+  const int grid = (int)(groups < n_sm ? groups : n_sm);
+  auto kern = f16 ? ftc_tc_kernel<true, true> : ftc_tc_kernel<false, true>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (e != cudaSuccess) return e;
   kern<<<grid, kTcThreads, kTcSmem, s>>>(p);

@@ -103,10 +103,11 @@ typedef struct {
   uint32_t overlap;            /* 1 = size the kernels so that the FT convolution of one
                                   buffer set and the harmonic summing of the other run
                                   concurrently on every SM (for pipelined A/B searches) */
-  uint32_t precision;          /* inverse DFT of the FT convolution: 0 = FP32 FFT on the
-                                  CUDA cores (default); 1 / 2 = DFT-64 x DFT-32 factor
-                                  products on the tensor cores (tcgen05) with split
-                                  (hi + lo) BF16 / FP16 operands, FP32 accumulation */
+  uint32_t precision;          /* the forward DFT of the tiles and the inverse DFT of the
+                                  FT convolution: 0 = FP32 FFTs on the CUDA cores
+                                  (default); 1 / 2 = DFT-64 x DFT-32 factor products on
+                                  the tensor cores (tcgen05) with split (hi + lo) BF16 /
+                                  FP16 operands, FP32 accumulation */
   uint32_t trace_enqueue;      /* 1 = fdas_launch logs the reference's per-launch host trace:
                                   "[INFO] Enqueueing: A" with the enqueue times of its
                                   stages in ms, and "%%%,A,t0,t1,t2,t3,t4," with the

@@ -3,8 +3,8 @@ the FP64 oracle (ft_conv.py:199-207 + hsum.py:95-151 in float64) and against
 the plain path:
 
 * precision form at 2^21 bins (the benchmark spectrum), split FP16 and split
-  BF16 on tcgen05: candidate set equal to the FP64 oracle's, FOP within its
-  tolerance (split FP16: the FP32 path's; split BF16: ten times it);
+  BF16 on tcgen05 (forward and inverse DFTs): candidate set equal to the FP64
+  oracle's, FOP within bounds twice the measured errors;
 * batched form over the 256-trial mix (2^17 .. 2^21 bins, log-uniform),
   autotuned: every trial's candidates equal to its own plain search, six
   trials (the shortest, the longest and four more) equal to the FP64 oracle;
@@ -62,11 +62,12 @@ def test_precision_full_size_vs_fp64(precision):
     print(f"FOP error: max |d| / plane mean {np.max(err / mean):.2e}, over cells below 30x the mean "
           f"{np.max((err / mean)[weak]):.2e}, max |d| / |FOP| over the others {np.max((err / fop64)[~weak]):.2e}, "
           f"within the FP32 path's tolerance: {fop_within(fop, fop64).mean():.9f} of the cells")
-    # measured bounds of the split forms at this size (the FP32 FFT meets
-    # 1e-5 x mean + 1e-6 x |FOP|, test_full_size_properties): the tensor-core
-    # products carry the rounding of the tile's largest values (the injected
-    # signals, ~10^4 x the mean) into the weak cells of the same tiles
-    a, b = (5e-5, 2e-6) if precision == 2 else (5e-4, 2e-5)
+    # bounds of the split forms at this size, twice the measured errors (the
+    # FP32 FFT meets 1e-5 x mean + 1e-6 x |FOP|, test_full_size_properties):
+    # the tensor-core products carry the rounding of a tile's largest values
+    # (the injected signals, ~10^4 x the mean) into the weak cells of the
+    # same tile, in the forward and in the inverse DFT
+    a, b = (1e-4, 4e-6) if precision == 2 else (2e-3, 6e-5)
     assert (err <= a * mean + b * np.abs(fop64)).all()
 
 

@@ -1,12 +1,13 @@
-"""Precision form (fdas_config.precision): the inverse DFT of the FT
-convolution as DFT-64 x DFT-32 factor products on the tensor cores (tcgen05)
-with split (hi + lo) BF16 or FP16 operands, against the FP64 oracle.
+"""Precision form (fdas_config.precision): the forward DFT of the tiles and
+the inverse DFT of the FT convolution as DFT-64 x DFT-32 factor products on
+the tensor cores (tcgen05) with split (hi + lo) BF16 or FP16 operands, against
+the FP64 oracle.
 
-Per stage against FP64: the tiles (forward FFT, FP32 on the CUDA cores in all
-forms) and the FOP (inverse DFT + power).  Split FP16 (22 significant bits)
-meets the FOP tolerance of the FP32 path; split BF16 (16 bits) is held to a
-10x wider bound.  With the FP64 recheck both forms give the FP64 oracle's
-candidate set."""
+Per stage against FP64: the tiles (forward DFT) and the FOP (inverse DFT +
+power).  Split FP16 (22 significant bits) meets the tile and FOP tolerances of
+the FP32 path at these sizes; split BF16 (16 bits) is held to measured wider
+bounds (tiles 3e-5 of the rms, FOP ten times the FP32 path's).  With the FP64
+recheck both forms give the FP64 oracle's candidate set."""
 import io
 
 import numpy as np
@@ -62,7 +63,7 @@ def test_precision_fop_per_stage(name):
         t_err, f_max, f_rms, ref = stage_errors(x, bank64, tiles, fop)
         print(f"{name} {NAMES[precision]}: tiles max |d| / rms {t_err:.2e}; "
               f"FOP |d| / plane mean: max {f_max:.2e}, rms {f_rms:.2e}")
-        assert t_err < 1e-5
+        assert t_err < (3e-5 if precision == 1 else 1e-5)  # split BF16 forward DFT: 1.8e-5 measured
         if precision in (0, 2):
             assert fop_within(fop, ref, x, bank64).all()
         else:  # split BF16: ten times the FP32 path's bound (1e-4 of the plane mean + 1e-4 of the cell)
