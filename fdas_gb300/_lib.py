@@ -19,6 +19,7 @@ STATUS_NAMES = ["OK", "INVALID_ARG", "OUT_OF_MEMORY", "CUDA", "TIMEOUT", "UNSUPP
 
 # fdas_set_fault_injection flags
 INJECT_FTC_STALL = 1
+INJECT_HSUM_STALL = 2
 
 # fdas_template_layout
 TEMPLATES_FFT_P4, TEMPLATES_FFT_NATURAL, TEMPLATES_TIME_DOMAIN = 0, 1, 2

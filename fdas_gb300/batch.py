@@ -75,11 +75,12 @@ class Batch:
         return FDAS.view(h)
 
     def info(self):
-        v = (ctypes.c_int32 * 6)()
+        v = (ctypes.c_int32 * 7)()
         ms = (ctypes.c_float * 16)()
-        self._lib.fdas_batch_info(self._b, v, 6, ms, 16)
+        self._lib.fdas_batch_info(self._b, v, 7, ms, 16)
         return {"ftc_split": "warp pair 32x64" if v[0] == 2 else "one warp 64x32", "ftc_ctas_per_sm": v[1],
-                "hsum_lean": bool(v[2]), "tuned": bool(v[3]), "tiles": v[4], "tune_ms": list(ms)[:v[5]]}
+                "hsum_lean": bool(v[2]), "tuned": bool(v[3]), "tiles": v[4], "tune_ms": list(ms)[:v[5]],
+                "ftc_launches": v[6]}
 
     def set_tuning(self, ftc_split, ftc_ctas_per_sm, hsum_lean):
         self._ok(self._lib.fdas_batch_set_tuning(self._b, int(ftc_split), int(ftc_ctas_per_sm), int(bool(hsum_lean))),

@@ -370,6 +370,7 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
   hsum_geometry(h, p);
   p.item_counter = S.d_ctrl + kCtrlItems;
   p.lean = h->cfg.overlap && P <= 8 && hsum_warps(H) == 11 ? 1 : 0;
+  p.inject_stall = (h->inject & FDAS_INJECT_HSUM_STALL) ? 1 : 0;
   p.cand_key = S.d_key;
   p.cand_pwr = S.d_pwr;
   p.cand_total = S.d_ctrl + kCtrlTotal;
@@ -1253,7 +1254,8 @@ void fdas_print_events(fdas_handle *h, fdas_buffer_set ab) {
 
 fdas_status fdas_set_fault_injection(fdas_handle *h, uint32_t flags) {
   CHECK_HANDLE(h);
-  if (flags & ~(uint32_t)FDAS_INJECT_FTC_STALL) return fail(h, FDAS_ERR_INVALID_ARG, "unknown injection flag");
+  if (flags & ~(uint32_t)(FDAS_INJECT_FTC_STALL | FDAS_INJECT_HSUM_STALL))
+    return fail(h, FDAS_ERR_INVALID_ARG, "unknown injection flag");
   h->inject = flags;
   return FDAS_OK;
 }
@@ -1340,6 +1342,7 @@ struct fdas_batch {
   cudaGraphExec_t exec = nullptr;
   std::vector<float> graph_thr;
   int ftc_variant = 2, ftc_ctas = 2, hsum_lean = 0;
+  int groups = 16;  // FT-convolution launches (1: the whole (trial, tile, template) queue in one)
   bool tuned = false;
   std::vector<float> tune_ms;
   std::string err;
@@ -1424,10 +1427,11 @@ fdas_status batch_enqueue(fdas_batch *b, const float *thr) {
   fp.n_trials = b->n_trials;
   // groups of consecutive trials with about equal numbers of tiles
   int i0 = 0;
-  for (int g = 0; g < (int)b->forks.size() && i0 < b->n_trials; ++g) {
-    const long long target = b->total_tiles * (g + 1) / (long long)b->forks.size();
+  const int n_groups = std::max(1, std::min(b->groups, (int)b->forks.size()));
+  for (int g = 0; g < n_groups && i0 < b->n_trials; ++g) {
+    const long long target = b->total_tiles * (g + 1) / (long long)n_groups;
     int i1 = i0 + 1;
-    while (i1 < b->n_trials && (g + 1 == (int)b->forks.size() || b->trials[i1].tile_begin < target)) ++i1;
+    while (i1 < b->n_trials && (g + 1 == n_groups || b->trials[i1].tile_begin < target)) ++i1;
     const long long t_lo = b->trials[i0].tile_begin;
     const long long t_hi = i1 < b->n_trials ? b->trials[i1].tile_begin : b->total_tiles;
     FtcParams gp = fp;
@@ -1489,10 +1493,16 @@ fdas_status batch_time(fdas_batch *b, const float *thr, float *ms) {
 }
 
 fdas_status batch_autotune(fdas_batch *b, const float *thr) {
+  // FFT split (radix 32 x 64 over a warp pair, or 64 x 32 in one warp),
+  // FT-convolution CTAs per SM (templates in flight per SM: 4 per CTA),
+  // harmonic-summing depth, and the grouping of the FT convolution: 16
+  // launches, 4, or one persistent launch over the whole (trial, tile,
+  // template) queue
   struct Cfg {
-    int variant, ctas, lean;
+    int variant, ctas, lean, groups;
   };
-  const Cfg cands[] = {{2, 2, 0}, {2, 1, 0}, {1, 1, 0}, {2, 2, 1}, {2, 1, 1}, {1, 1, 1}};
+  const Cfg cands[] = {{2, 2, 0, 16}, {2, 1, 0, 16}, {1, 1, 0, 16}, {2, 2, 1, 16},
+                       {2, 1, 1, 16}, {1, 1, 1, 16}, {2, 2, 0, 4},  {2, 2, 0, 1}};
   float best = 1e30f;
   Cfg pick = cands[0];
   b->tune_ms.clear();
@@ -1500,6 +1510,7 @@ fdas_status batch_autotune(fdas_batch *b, const float *thr) {
     b->ftc_variant = c.variant;
     b->ftc_ctas = c.ctas;
     b->hsum_lean = c.lean;
+    b->groups = c.groups;
     float ms = 0.f;
     fdas_status st = batch_time(b, thr, &ms);
     if (st != FDAS_OK) return st;
@@ -1512,6 +1523,7 @@ fdas_status batch_autotune(fdas_batch *b, const float *thr) {
   b->ftc_variant = pick.variant;
   b->ftc_ctas = pick.ctas;
   b->hsum_lean = pick.lean;
+  b->groups = pick.groups;
   b->tuned = true;
   return FDAS_OK;
 }
@@ -1761,9 +1773,9 @@ fdas_handle *fdas_batch_trial(fdas_batch *b, uint32_t trial) {
 
 fdas_status fdas_batch_info(fdas_batch *b, int32_t *out, uint32_t n, float *tune_ms, uint32_t n_ms) {
   if (!b) return FDAS_ERR_INVALID_ARG;
-  const int32_t v[6] = {b->ftc_variant, b->ftc_ctas, b->hsum_lean, b->tuned ? 1 : 0, (int32_t)b->total_tiles,
-                        (int32_t)b->tune_ms.size()};
-  for (uint32_t i = 0; out && i < n && i < 6; ++i) out[i] = v[i];
+  const int32_t v[7] = {b->ftc_variant, b->ftc_ctas, b->hsum_lean, b->tuned ? 1 : 0, (int32_t)b->total_tiles,
+                        (int32_t)b->tune_ms.size(), b->groups};
+  for (uint32_t i = 0; out && i < n && i < 7; ++i) out[i] = v[i];
   for (uint32_t i = 0; tune_ms && i < n_ms && i < b->tune_ms.size(); ++i) tune_ms[i] = b->tune_ms[i];
   return FDAS_OK;
 }

@@ -133,6 +133,8 @@ struct HsumParams {
   int *status;
   long long timeout_ns;   // bound on every wait
   int lean;               // 1: 3 stages and <= 80 registers (shares an SM with the FT convolution)
+  int inject_stall = 0;   // test hook: the first stage of every CTA is announced on its barriers
+                          // but its copies are not issued, so the consumers' waits run out
 };
 
 // 2-D tensor maps of the FOP (rows x stride floats), one box shape per plane

@@ -406,7 +406,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
               drained &= mbar_wait_parity(full2 + q, pending[q] & 1, kDrainNs);
               pending[q] = -1;
             }
-          if (drained) {
+          // (a stage the test hook announced without copies has a phase that
+          // never completes: no stop mark on it -- its consumers have left)
+          if (drained && !(p.inject_stall && st == 0)) {
             item_id[st] = -1;
             mbar_arrive(full + st);
           }
@@ -427,12 +429,17 @@ __global__ void __launch_bounds__(32 * (NW + 1), MINB) hsum_kernel(const __grid_
           break;
         }
         item_id[st] = it;
+        const unsigned bytes1 = (unsigned)(p.bw[1] * p.bh[1]) * 4u;
+        if (p.inject_stall && s == 0) {  // test hook: announced, never issued -- nothing in flight
+          mbar_arrive_expect_tx(full + st, bytes1);
+          mbar_arrive_expect_tx(full2 + st, p.stage_bytes - bytes1 + 16u);
+          continue;
+        }
 #pragma unroll
         for (int q = 0; q < kHsStages; ++q)
           if (q == st) pending[q] = use;
         const HsItem item = hs_item(p, it);
         float *stage = stages + st * p.stage_floats;
-        const unsigned bytes1 = (unsigned)(p.bw[1] * p.bh[1]) * 4u;
         mbar_arrive_expect_tx(full + st, bytes1);
         tma_load_2d(stage + p.soff[1], &m.map[1], item.f0, item.sgn > 0 ? H : H - (kRows1 - 1), full + st);
         mbar_arrive_expect_tx(full2 + st, p.stage_bytes - bytes1);  // 0 bytes with one plane: a plain arrival

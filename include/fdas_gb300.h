@@ -275,14 +275,17 @@ void fdas_set_log(fdas_handle *h, fdas_log_fn fn, void *user);
  * waits have no bound). */
 fdas_status fdas_set_wait_timeout(fdas_handle *h, int64_t ns);
 
-/* Test hook for the timeout path (no counterpart in the reference).  With
+/* Test hooks for the timeout paths (no counterpart in the reference).  With
  * FDAS_INJECT_FTC_STALL set, the FT convolution of later searches announces
  * each warp pair's first template copy on its barrier but never issues it, so
  * that wait cannot complete and runs out after the bound of
  * fdas_set_wait_timeout: the search stops with the FT-convolution timeout bit
- * and fdas_wait returns FDAS_ERR_TIMEOUT.  No memory access is made or left
- * in flight by the hook; 0 switches it off. */
+ * and fdas_wait returns FDAS_ERR_TIMEOUT.  FDAS_INJECT_HSUM_STALL does the
+ * same to the first staged item of every harmonic-summing CTA (status bit 1).
+ * No memory access is made or left in flight by the hooks; 0 switches them
+ * off. */
 #define FDAS_INJECT_FTC_STALL 1u
+#define FDAS_INJECT_HSUM_STALL 2u
 fdas_status fdas_set_fault_injection(fdas_handle *h, uint32_t flags);
 
 /* Stage times of the last completed launch on `ab`, in milliseconds:
@@ -493,7 +496,9 @@ fdas_status fdas_batch_wait(fdas_batch *b);
 fdas_handle *fdas_batch_trial(fdas_batch *b, uint32_t trial);
 /* out: [0] FFT split (1 one warp, 2 warp pair), [1] FT-convolution CTAs per SM,
  * [2] lean harmonic summing, [3] tuned, [4] tiles of the batch, [5] configs
- * timed; tune_ms: the autotuner's time per configuration. */
+ * timed, [6] FT-convolution launches the trials are grouped into (1: one
+ * persistent launch over the whole (trial, tile, template) queue); tune_ms:
+ * the autotuner's time per configuration. */
 fdas_status fdas_batch_info(fdas_batch *b, int32_t *out, uint32_t n, float *tune_ms, uint32_t n_ms);
 /* Fix the tuning by hand (skips the autotuner; the graph is recaptured). */
 fdas_status fdas_batch_set_tuning(fdas_batch *b, int32_t ftc_variant, int32_t ftc_ctas_per_sm, int32_t hsum_lean);

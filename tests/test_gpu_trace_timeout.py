@@ -124,11 +124,15 @@ def _search(p, x, thr):
     return ok, loc, pwr
 
 
-def test_device_wait_timeout_reported_and_recovered():
-    """A device wait that runs out: the test hook announces each warp pair's
-    first template copy of the FT convolution without issuing it, so that
-    wait can never complete.  After the (shortened) bound the kernel stops,
-    the search reports FDAS_ERR_TIMEOUT with the FT-convolution timeout bit,
+@pytest.mark.parametrize("hook,bit,what", [(_lib.INJECT_FTC_STALL, 16, "FT convolution"),
+                                           (_lib.INJECT_HSUM_STALL, 1, "harmonic summing")],
+                         ids=["ft_convolution", "harmonic_summing"])
+def test_device_wait_timeout_reported_and_recovered(hook, bit, what):
+    """A device wait that runs out: a test hook announces copies on a barrier
+    without issuing them (each warp pair's first template copy of the FT
+    convolution, or the first staged item of every harmonic-summing CTA), so
+    that wait can never complete.  After the (shortened) bound the kernel
+    stops, the search reports FDAS_ERR_TIMEOUT with the stage's timeout bit,
     and once the hook is off the next searches on the same handle are exact
     again -- the context stays usable."""
     x, thr = _case(n=1 << 15, seed=5)
@@ -142,16 +146,16 @@ def test_device_wait_timeout_reported_and_recovered():
     p = make_pipeline(x.size, log=io.StringIO())
     assert p.upload_templates(bank, FDAS.A)
     assert p.set_wait_timeout(1_000_000)  # 1 ms
-    assert p.set_fault_injection(_lib.INJECT_FTC_STALL)
+    assert p.set_fault_injection(hook)
     for _ in range(2):
         t0 = time.monotonic()
         ok, _, _ = _search(p, x, thr)
         assert not ok
         assert p.last_status == _lib.ERR_TIMEOUT, p.last_error
-        assert "FT convolution" in p.last_error
-        assert p.counters(FDAS.A)["status"] & 16
+        assert what in p.last_error
+        assert p.counters(FDAS.A)["status"] & bit
         assert time.monotonic() - t0 < 1.5  # the bound, not the 2 s default, ended the wait
-    assert not p.set_fault_injection(2)  # unknown flags are refused
+    assert not p.set_fault_injection(4)  # unknown flags are refused
     assert p.set_fault_injection(0)
     assert p.set_wait_timeout(0)  # back to 2 s
     for _ in range(2):
