@@ -389,7 +389,7 @@ def run_ours(args):
         # their own workloads (each reports the plain path it is compared with)
         p.close()
         q.close()
-        forms = {"batched": batched_form(256, steps=3, warmup=2),
+        forms = {"batched": batched_form(256, steps=3, warmup=3),
                  "served": [served_form(rate, 400, 8) for rate in (400.0, 2000.0)],
                  "precision": precision_form(N_BINS, steps=20, warmup=3)}
     line = {

@@ -45,29 +45,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
       : "memory");
   return done != 0;
 }
-// TMA bulk copy global -> shared, completion signalled on the mbarrier
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
 __device__ __forceinline__ uint64_t globaltimer_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
-// Bounded wait on phase 0 of the barrier; false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, long long timeout_ns) {
-  if (mbar_try_wait(bar, 0)) return true;
-  const uint64_t t0 = globaltimer_ns();
-  while (true) {
-    if (mbar_try_wait(bar, 0)) return true;
-    if ((long long)(globaltimer_ns() - t0) > timeout_ns) return false;
-  }
-}
-
 // one record appended to the global list (single-thread use)
 __device__ __forceinline__ void global_append(unsigned long long *keys, float *pwrs, unsigned *total, int cap,
                                               int *status, unsigned long long key, float pwr) {
