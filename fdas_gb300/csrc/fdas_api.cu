@@ -85,6 +85,9 @@ struct BufferSet {
   bool ev_ftc_recorded = false;
   bool ftc_unchecked = false;  // an FT convolution ran whose status word has not been checked
   bool tile_unchecked = false; // a tensor-core tiling ran whose status word has not been checked
+  cudaEvent_t ev_hsum = nullptr;  // end of this set's last harmonic-summing kernel
+  bool ev_hsum_recorded = false;
+  bool input_from_host = false;   // the current spectrum was copied in from host memory
 };
 
 }  // namespace
@@ -263,6 +266,7 @@ fdas_status enqueue_input(fdas_handle *h, int ab, const fdas_complex *input, boo
   CK(h, cudaEventRecord(S.ev[0], S.stream));
   if (h->cfg.sync_pipeline && h->set[1 - ab].ev_ftc_recorded)
     CK(h, cudaStreamWaitEvent(S.stream, h->set[1 - ab].ev[3], 0));  // FDAS.cpp:287-288
+  S.input_from_host = false;
   if (!input) {
     S.cur_input = S.d_input;
   } else if (device_ptr) {
@@ -271,6 +275,7 @@ fdas_status enqueue_input(fdas_handle *h, int ab, const fdas_complex *input, boo
     CK(h, cudaMemcpyAsync(S.d_input, input, sizeof(float2) * (size_t)h->N, cudaMemcpyHostToDevice, S.stream));
     S.cur_input = S.d_input;
     S.series_spectrum = false;
+    S.input_from_host = true;
   }
   CK(h, cudaEventRecord(S.ev[1], S.stream));
   S.have_input = true;
@@ -324,6 +329,16 @@ fdas_status enqueue_ftc(fdas_handle *h, int ab, fdas_fop_part which) {
     p.variant = 2;  // the hook lives in the warp-pair FFT kernel
   }
   S.ctrl_valid = false;  // the host copy of the control words predates this stage
+  // A search whose spectrum was copied from host memory starts its FT
+  // convolution only once the other set's harmonic-summing kernel has ended.
+  // Otherwise that harmonic summing finds every SM held by this FT convolution
+  // (two CTAs of 128 registers x 256 threads fill an SM's register file), both
+  // searches end together, and with launch(A) / wait(B) the next launch -- its
+  // 16 MB copy and tiling -- starts on an empty GPU every second search.
+  // Device-resident searches queued ahead keep the unordered form, where the
+  // two harmonic summings run side by side after both FT convolutions.
+  if (S.input_from_host && !h->cfg.overlap && !h->cfg.sync_pipeline && h->set[1 - ab].ev_hsum_recorded)
+    CK(h, cudaStreamWaitEvent(S.stream, h->set[1 - ab].ev_hsum, 0));
   CK(h, cudaMemsetAsync(S.d_ctrl + kCtrlFtcStatus, 0, sizeof(unsigned), S.stream));
   CK(h, launch_ftc(p, S.stream));
   CK(h, cudaEventRecord(S.ev[3], S.stream));
@@ -386,6 +401,10 @@ fdas_status enqueue_hsum(fdas_handle *h, int ab, const float *thr_in, fdas_fop_p
     return fail(h, FDAS_ERR_UNSUPPORTED, "harmonic summing staging exceeds shared memory (too many templates x planes)");
   CK(h, cudaMemsetAsync(S.d_ctrl, 0, sizeof(unsigned) * kCtrlWords, S.stream));
   CK(h, launch_hsum(p, S.maps, S.stream));
+  if (S.ev_hsum) {  // (the batched form's per-trial views have none)
+    CK(h, cudaEventRecord(S.ev_hsum, S.stream));
+    S.ev_hsum_recorded = true;
+  }
   if (recheck) {
     RecheckParams r{};
     r.input = S.cur_input;
@@ -508,6 +527,7 @@ void free_set(BufferSet &S) {
   if (S.h_ctrl) cudaFreeHost(S.h_ctrl);
   for (auto &e : S.ev)
     if (e) cudaEventDestroy(e);
+  if (S.ev_hsum) cudaEventDestroy(S.ev_hsum);
   if (S.stream) cudaStreamDestroy(S.stream);
   S = BufferSet();
 }
@@ -677,6 +697,10 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
         cuda_fail(h, e, "cudaEventCreate", __FILE__, __LINE__);
         return bail(FDAS_ERR_CUDA);
       }
+    }
+    if ((e = cudaEventCreateWithFlags(&S.ev_hsum, cudaEventDisableTiming)) != cudaSuccess) {
+      cuda_fail(h, e, "cudaEventCreate", __FILE__, __LINE__);
+      return bail(FDAS_ERR_CUDA);
     }
   }
   // the anchor placing device events on the host's steady clock

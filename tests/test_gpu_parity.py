@@ -291,6 +291,61 @@ def test_drive_pipelined():
     assert p.wait(FDAS.A)
 
 
+def test_alternating_host_and_device_inputs():
+    """The A/B driver loop (launch one set, wait for the other) over different
+    spectra, host-memory launches (whose FT convolution is ordered after the
+    other set's harmonic summing) mixed with device-resident ones (unordered)
+    on one handle: every search's candidate list equals the same spectrum's
+    searched alone."""
+    import torch
+    n = 1 << 16
+    bank = template_bank()
+    thr = O.chi2_thresholds(1e-6)
+    specs = []
+    for i in range(9):
+        rng = np.random.default_rng(100 + i)
+        sig = [dict(r0=float(rng.uniform(0.05, 0.45) * n), z=float(rng.uniform(-40, 40)),
+                    n_harm=int(rng.integers(1, 9)), amp=0.02) for _ in range(2)]
+        specs.append(synth.spectrum(synth.timeseries(2 * n, sig, seed=100 + i), n)[0])
+    alone = make_pipeline(n, log=io.StringIO())
+    assert alone.upload_templates(bank, FDAS.A)
+    nc = alone.get_candidate_list_sz()
+    want = []
+    for x in specs:
+        loc, pwr = np.zeros(nc, np.uint32), np.zeros(nc, np.float32)
+        assert alone.launch(x, thr, loc, pwr, FDAS.AllAccelerations, FDAS.A) and alone.wait(FDAS.A)
+        rec, _, dropped = alone.retrieve_candidate_list(FDAS.A)
+        assert dropped == 0 and rec.size > 0
+        want.append((rec, loc, pwr))
+    alone.close()
+
+    p = make_pipeline(n, log=io.StringIO())
+    assert p.upload_templates(bank, FDAS.A) and p.upload_templates(bank, FDAS.B)
+    on_device = [i % 3 == 2 for i in range(len(specs))]
+    d_specs = [torch.from_numpy(x.view(np.float32)).cuda() if dev else None for x, dev in zip(specs, on_device)]
+    outs = [(np.zeros(nc, np.uint32), np.zeros(nc, np.float32)) for _ in specs]
+
+    def finish(j):
+        ab = j & 1
+        assert (p.synchronize(ab) if on_device[j] else p.wait(ab)), p.last_error
+        rec, _, dropped = p.retrieve_candidate_list(ab)
+        assert dropped == 0
+        assert np.array_equal(rec, want[j][0]), j
+        if not on_device[j]:
+            assert np.array_equal(outs[j][0], want[j][1]) and np.array_equal(outs[j][1], want[j][2]), j
+
+    for i, x in enumerate(specs):
+        ab = i & 1
+        if on_device[i]:
+            assert p.enqueue_search_device(d_specs[i].data_ptr(), thr, FDAS.AllAccelerations, ab), p.last_error
+        else:
+            assert p.launch(x, thr, outs[i][0], outs[i][1], FDAS.AllAccelerations, ab), p.last_error
+        if i > 0:
+            finish(i - 1)
+    finish(len(specs) - 1)
+    p.close()
+
+
 @pytest.mark.parametrize("n_bins", [1, 7, 1627, 1628, 1629, 3001, 2 * 1628 + 1])
 def test_edge_sizes(n_bins, bank64):
     """Ragged sizes: a single bin, a partial first tile, exact tile multiples."""
