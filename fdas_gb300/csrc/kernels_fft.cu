@@ -1,5 +1,6 @@
 // (a) overlap-save tiling + forward FFT, (c) fused template multiply,
 // inverse FFT, power and overlap discard, and the FP64 template precompute.
+#include <climits>
 #include <cstdlib>
 #include <cstring>
 
@@ -104,34 +105,51 @@ struct FopTarget {
   long long base;
   int n_bins;
 };
-// Trial of the launch's tile `tile` (batched search; 0 otherwise).  Looked up
-// when the item starts, so the search's dependent loads overlap the FFT.
-template <bool BATCH>
-__device__ __forceinline__ int trial_of(const FtcParams &p, int tile) {
-  if constexpr (!BATCH) return 0;
-  return batch_trial_of(p.trials, p.n_trials, p.tile_begin + tile);  // the launch may cover a range of tiles
+// The trial of a warp's (or pair's) current item in the batched search, its
+// fields held in registers.  A warp's items only move forward (item += grid
+// size), so after one binary search at the first item the trial is found by
+// walking forward from the previous one -- usually no step at all -- instead
+// of a dependent chain of loads per item.
+struct TrialCursor {
+  long long next_begin;  // first global tile of the next trial
+  long long tile_begin;  // first global tile of this trial
+  long long fop_offset;
+  long long stride;
+  int t;
+  int n_bins;
+};
+__device__ __forceinline__ void cursor_load(const FtcParams &p, TrialCursor &c) {
+  const BatchTrial &tr = p.trials[c.t];
+  c.tile_begin = tr.tile_begin;
+  c.fop_offset = tr.fop_offset;
+  c.stride = tr.stride;
+  c.n_bins = tr.n_bins;
+  c.next_begin = c.t + 1 < p.n_trials ? p.trials[c.t + 1].tile_begin : LLONG_MAX;
 }
 template <bool BATCH>
-__device__ __forceinline__ FopTarget fop_target(const FtcParams &p, int tile, int row, int trial) {
+__device__ __forceinline__ void cursor_start(const FtcParams &p, int tile, TrialCursor &c) {
+  if constexpr (BATCH) {
+    c.t = batch_trial_of(p.trials, p.n_trials, p.tile_begin + tile);  // the launch may cover a range of tiles
+    cursor_load(p, c);
+  }
+}
+template <bool BATCH>
+__device__ __forceinline__ void cursor_seek(const FtcParams &p, int tile, TrialCursor &c) {
+  if constexpr (BATCH) {
+    while (p.tile_begin + tile >= c.next_begin) {
+      ++c.t;
+      cursor_load(p, c);
+    }
+  }
+}
+template <bool BATCH>
+__device__ __forceinline__ FopTarget fop_target(const FtcParams &p, int tile, int row, const TrialCursor &c) {
   if constexpr (!BATCH)
     return FopTarget{p.fop + (long long)row * p.fop_stride, (long long)tile * p.payload - p.overlap, p.n_bins};
-  const BatchTrial &tr = p.trials[trial];
-  return FopTarget{p.fop + tr.fop_offset + (long long)row * tr.stride,
-                   (p.tile_begin + tile - tr.tile_begin) * p.payload - p.overlap, tr.n_bins};
+  return FopTarget{p.fop + c.fop_offset + (long long)row * c.stride,
+                   (p.tile_begin + tile - c.tile_begin) * p.payload - p.overlap, c.n_bins};
 }
 
-// Persistent: one CTA of 8 warps per SM; each warp loops over (tile,
-// template) items, item = tile * n_rows + r, so the 8 warps of a CTA usually
-// share the tile operand in L1 while their phases drift apart.  The next
-// item's template spectrum is prefetched by a 16 KB TMA bulk copy into the
-// warp's exchange buffer as soon as the exchange has been read back, so it
-// lands during the second FFT pass.
-// Per item: Y = S_tile * T_tmpl (templates carry the 1/2048 of the inverse
-// transform, so |y|^2 already includes the reference's power normalisation by
-// 2048^2, utils.cl.mako:41-47); y = IFFT(Y);
-// FOP[row][i P + n - O] = |y[n]|^2 for n >= O, trimmed to N bins
-// (square_and_discard.cl.mako:28-76).
-// BATCH: tiles of several trials (trial table), else one spectrum's tiles
 template <bool BATCH>
 __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
   extern __shared__ float4 smem_f4[];
@@ -151,10 +169,12 @@ __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
   if (item < n_items && lane == 0)
     prefetch_template(ex, p.tmpl + (long long)(p.row_begin + item % p.n_rows) * kTile, bar);
   uint32_t parity = 0;
+  TrialCursor cur;
+  if (item < n_items) cursor_start<BATCH>(p, item / p.n_rows, cur);
   for (; item < n_items; item += stride) {
     const int tile = item / p.n_rows;
     const int row = p.row_begin + (item - tile * p.n_rows);
-    const int trial = trial_of<BATCH>(p, tile);
+    cursor_seek<BATCH>(p, tile, cur);
     const float2 *s = p.tiles + (long long)tile * kTile + lane;
     float2 v[64];
     sfor<64>([&](auto K) {
@@ -177,7 +197,7 @@ __global__ void __launch_bounds__(256, 1) ftc_kernel(FtcParams p) {
       if (next < n_items && lane == 0)
         prefetch_template(ex, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
     });
-    const FopTarget tg = fop_target<BATCH>(p, tile, row, trial);
+    const FopTarget tg = fop_target<BATCH>(p, tile, row, cur);
     sfor<2>([&](auto C) {
       constexpr int c = decltype(C)::value;
       sfor<32>([&](auto D) {
@@ -243,10 +263,12 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
   uint32_t parity = 0;
   const int m = 16 * h + (lane & 15);
   const int g = lane >> 4;
+  TrialCursor cur;
+  if (item < n_items) cursor_start<BATCH>(p, item / p.n_rows, cur);
   for (; item < n_items; item += stride) {
     const int tile = item / p.n_rows;
     const int row = p.row_begin + (item - tile * p.n_rows);
-    const int trial = trial_of<BATCH>(p, tile);
+    cursor_seek<BATCH>(p, tile, cur);
     const float2 *s = p.tiles + (long long)tile * kTile + tp;
     float2 v[32];
     sfor<32>([&](auto A) {
@@ -275,7 +297,7 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
       if (next < n_items && tp == 0)
         prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
     });
-    const FopTarget tg = fop_target<BATCH>(p, tile, row, trial);
+    const FopTarget tg = fop_target<BATCH>(p, tile, row, cur);
     sfor<4>([&](auto R) {
       constexpr int r = decltype(R)::value;
       sfor<8>([&](auto D2) {
