@@ -523,12 +523,15 @@ def served_form(rate, n_req, slots):
 
 
 # ------------------------------------------------------------------ batched form
-def batched_form(n_tr=256, steps=5, warmup=3, autotune=True):
+def batched_form(n_tr=256, steps=5, warmup=3, autotune=True, profile_one=False):
     """256 dedispersed trials of uneven length (log-uniform 2^18..2^22 samples,
     i.e. 2^17..2^21 bins), 0-2 accelerated signals each (z in [-42, 42], 1-8
     harmonics), 85-template bank, 8 planes, chi-square FAR 1e-6: one batched
-    pass (one FT-convolution launch over all trials' items, CUDA graph,
-    autotuned) against the plain path searching the same trials one by one."""
+    pass (persistent FT-convolution launches over all trials' items, CUDA
+    graph, autotuned) against the plain path searching the same trials one by
+    one and on two alternating handles.  ``profile_one``: after the timed
+    replays, one more replay between cudaProfilerStart and cudaProfilerStop,
+    for ``ncu --profile-from-start off``."""
     import torch
     from scipy.stats import gamma
     from fdas_gb300.batch import Batch
@@ -557,6 +560,12 @@ def batched_form(n_tr=256, steps=5, warmup=3, autotune=True):
         b.run(thr)
         times.append(time.perf_counter() - t)
     batched_s = float(np.median(times))
+    if profile_one:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        b.run(thr)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     info = b.info()
     n_cand = sum(b.trial(i).retrieve_candidate_list(FDAS.A, capacity=0)[1] for i in range(n_tr))
     b.close()
@@ -684,6 +693,8 @@ def main():
                     help="spectrum bins; the reported workload is 2^21, smaller values are for ncu captures")
     ap.add_argument("--trials", type=int, default=256, help="batched form: number of trials")
     ap.add_argument("--no-autotune", action="store_true", help="batched form: default tuning")
+    ap.add_argument("--profile-one", action="store_true",
+                    help="batched form: one extra replay inside cudaProfilerStart/Stop (ncu --profile-from-start off)")
     ap.add_argument("--form", default="plain", choices=["plain", "served", "batched", "precision"],
                     help="served: the request server under Poisson arrivals (prints its own JSON line)")
     ap.add_argument("--rate", type=float, default=200.0, help="served form: arrival rate (searches/s)")
@@ -699,7 +710,8 @@ def main():
         print(json.dumps(served_form(args.rate, args.requests, args.slots)), flush=True)
         return
     if args.form == "batched":
-        print(json.dumps(batched_form(args.trials, args.steps, args.warmup, not args.no_autotune)), flush=True)
+        print(json.dumps(batched_form(args.trials, args.steps, args.warmup, not args.no_autotune,
+                                      args.profile_one)), flush=True)
         return
     if args.form == "precision":
         print(json.dumps(precision_form(args.bins, args.steps, args.warmup, args.noise_only)), flush=True)
