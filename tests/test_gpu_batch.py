@@ -1,7 +1,8 @@
 """Batched form (fdas_batch_*): trials of uneven length searched in one pass
-(one tiling launch, one persistent FT-convolution launch over all trials'
-(tile, template) items, per-trial harmonic summing on branch streams, all in
-one CUDA graph) against plain searches of each trial on its own handle."""
+(one tiling launch, persistent FT-convolution launches over all trials'
+(tile, template) items -- one, or one per group of trials, as tuned --
+per-trial harmonic summing on branch streams, all in one CUDA graph) against
+plain searches of each trial on its own handle."""
 import io
 
 import numpy as np
