@@ -116,6 +116,7 @@ SIGNATURES = {
     "fdas_batch_trial": (_P, [_P, _U32]),
     "fdas_batch_info": (_INT, [_P, _P, _U32, _P, _U32]),
     "fdas_batch_set_tuning": (_INT, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "fdas_batch_set_groups": (_INT, [_P, ctypes.c_int32]),
     "fdas_batch_last_error": (ctypes.c_char_p, [_P]),
     "fdas_batch_destroy": (None, [_P]),
     "fdas_reshape": (_INT, [_P, _U32, _U32, _U32, _U32, _U32]),

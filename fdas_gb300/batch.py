@@ -86,6 +86,11 @@ class Batch:
         self._ok(self._lib.fdas_batch_set_tuning(self._b, int(ftc_split), int(ftc_ctas_per_sm), int(bool(hsum_lean))),
                  "set_tuning")
 
+    def set_groups(self, groups):
+        """FT-convolution launches the trials are grouped into (1..16; 1: one
+        persistent launch over the whole queue); skips the autotuner."""
+        self._ok(self._lib.fdas_batch_set_groups(self._b, int(groups)), "set_groups")
+
     def close(self):
         if self._b:
             self._lib.fdas_batch_destroy(self._b)

@@ -1818,6 +1818,17 @@ fdas_status fdas_batch_set_tuning(fdas_batch *b, int32_t ftc_variant, int32_t ft
   return FDAS_OK;
 }
 
+fdas_status fdas_batch_set_groups(fdas_batch *b, int32_t groups) {
+  if (!b || groups < 1 || groups > kBatchGroups) return bfail(b, FDAS_ERR_INVALID_ARG, "groups must be 1..16");
+  b->groups = groups;
+  b->tuned = true;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  return FDAS_OK;
+}
+
 const char *fdas_batch_last_error(const fdas_batch *b) { return b ? b->err.c_str() : g_init_error.c_str(); }
 
 void fdas_batch_destroy(fdas_batch *b) {

@@ -502,6 +502,13 @@ fdas_handle *fdas_batch_trial(fdas_batch *b, uint32_t trial);
 fdas_status fdas_batch_info(fdas_batch *b, int32_t *out, uint32_t n, float *tune_ms, uint32_t n_ms);
 /* Fix the tuning by hand (skips the autotuner; the graph is recaptured). */
 fdas_status fdas_batch_set_tuning(fdas_batch *b, int32_t ftc_variant, int32_t ftc_ctas_per_sm, int32_t hsum_lean);
+/* Fix the grouping by hand: the trials are split into `groups` (1..16) runs of
+ * about equal tile counts, one FT-convolution launch each, whose harmonic
+ * summing starts while the next run's FT convolution runs (1: one persistent
+ * launch over the whole queue).  Skips the autotuner, like
+ * fdas_batch_set_tuning; the graph is recaptured.  Results do not depend on
+ * the grouping. */
+fdas_status fdas_batch_set_groups(fdas_batch *b, int32_t groups);
 const char *fdas_batch_last_error(const fdas_batch *b);
 void fdas_batch_destroy(fdas_batch *b);
 

@@ -98,3 +98,31 @@ def test_batch_autotuned_same_candidates(inputs):
             key = lambda r: list(zip(r["harmonic"], r["template_num"], r["bin"]))
             assert key(rec) == key(r_rec), i
             np.testing.assert_allclose(rec["power"], r_rec["power"], rtol=1e-5, atol=1e-5 * 8)
+
+
+@pytest.mark.parametrize("groups", [1, 4, 16])
+def test_batch_groupings_equal_plain(groups):
+    """Every grouping of the FT convolution (one launch over the whole
+    (trial, tile, template) queue, or one launch per run of trials; each warp
+    pair walks forward through the trial table of its launch) gives the plain
+    searches' FOPs and candidate lists bit for bit, also when trials outnumber
+    groups so that a launch spans several trials."""
+    bank = template_bank()
+    thr = O.chi2_thresholds(1e-6, 8)
+    n_bins = [1628 * 3 + 17, 20000, 4096, 70001, 1628, 33333, 9000, 131072, 2048, 50000, 1, 12345]
+    xs = [spectrum(n, 200 + i) if n > 1 else np.ones(1, np.complex64) for i, n in enumerate(n_bins)]
+    ref = [plain(x, bank, thr) for x in xs]
+    with Batch(bank, n_bins, autotune=False) as b:
+        b.set_tuning(2, 2, False)
+        b.set_groups(groups)
+        assert b.info()["ftc_launches"] == groups
+        b.set_inputs(xs)
+        b.run(thr)
+        for i in range(len(n_bins)):
+            rec, loc, pwr, fop = batch_results(b, i)
+            r_rec, r_loc, r_pwr, r_fop = ref[i]
+            assert np.array_equal(fop, r_fop), (groups, i)
+            assert np.array_equal(rec, r_rec), (groups, i)
+            assert np.array_equal(loc, r_loc) and np.array_equal(pwr, r_pwr), (groups, i)
+        with pytest.raises(RuntimeError):
+            b.set_groups(17)
