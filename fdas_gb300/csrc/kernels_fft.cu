@@ -263,11 +263,18 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
   uint32_t parity = 0;
   const int m = 16 * h + (lane & 15);
   const int g = lane >> 4;
+  // (tile, row) of the item, advanced by the grid stride without divisions
+  const int st_tiles = stride / p.n_rows, st_rows = stride - st_tiles * p.n_rows;
+  int tile = item / p.n_rows, rr = item - tile * p.n_rows;
   TrialCursor cur;
-  if (item < n_items) cursor_start<BATCH>(p, item / p.n_rows, cur);
+  if (item < n_items) cursor_start<BATCH>(p, tile, cur);
   for (; item < n_items; item += stride) {
-    const int tile = item / p.n_rows;
-    const int row = p.row_begin + (item - tile * p.n_rows);
+    const int row = p.row_begin + rr;
+    int next_tile = tile + st_tiles, next_rr = rr + st_rows;
+    if (next_rr >= p.n_rows) {
+      next_rr -= p.n_rows;
+      ++next_tile;
+    }
     cursor_seek<BATCH>(p, tile, cur);
     const float2 *s = p.tiles + (long long)tile * kTile + tp;
     float2 v[32];
@@ -295,18 +302,28 @@ __global__ void __launch_bounds__(256, 2) ftc2_kernel(FtcParams p) {
     ifft2_pass2(buf, h, lane, pw, [&]() {
       pair_sync(pair);  // exchange read by both warps: prefetch the next template
       if (next < n_items && tp == 0)
-        prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + next % p.n_rows) * kTile, bar);
+        prefetch_template(buf_f, p.tmpl + (long long)(p.row_begin + next_rr) * kTile, bar);
     });
+    // output n = m + 128 g + c, c = 32 r + 256 d2 known at compile time: the
+    // discard (n >= O) and the row end (bin < n_bins) become two 32-bit
+    // limits on c per thread and item
     const FopTarget tg = fop_target<BATCH>(p, tile, row, cur);
+    const int mb = m + 128 * g;
+    const long long first = tg.base + mb;  // bin of c = 0 (negative in the first tile)
+    const long long room = (long long)tg.n_bins - first;
+    const int lo = p.overlap - mb, hi = room < kTile ? (int)room : kTile;
+    const unsigned long long dst =
+        reinterpret_cast<unsigned long long>(tg.out) + 4ull * static_cast<unsigned long long>(first);
     sfor<4>([&](auto R) {
       constexpr int r = decltype(R)::value;
       sfor<8>([&](auto D2) {
         constexpr int d2 = decltype(D2)::value;
-        const int n = m + 32 * (4 * g + r) + 256 * d2;
-        const long long b = tg.base + n;
-        if (n >= p.overlap && b < tg.n_bins) tg.out[b] = pw[8 * r + d2];
+        constexpr int c = 32 * r + 256 * d2;
+        if (c >= lo && c < hi) *reinterpret_cast<float *>(dst + 4ull * c) = pw[8 * r + d2];
       });
     });
+    tile = next_tile;
+    rr = next_rr;
   }
 }
 
