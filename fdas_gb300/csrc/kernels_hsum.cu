@@ -691,10 +691,22 @@ __global__ void __launch_bounds__(1024) select_hist_kernel(SelectParams p) {
   extern __shared__ unsigned sh_hist[];  // [n_planes][kSelBuckets]
   __shared__ bool last;
   __shared__ bool over[kMaxPlanes];  // plane has more hits than K
+  __shared__ int n_over;
   const int nb = p.n_planes * kSelBuckets;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) sh_hist[i] = 0u;
-  if (threadIdx.x < kMaxPlanes)
+  if (threadIdx.x == 0) n_over = 0;
+  __syncthreads();
+  if (threadIdx.x < kMaxPlanes) {
     over[threadIdx.x] = threadIdx.x < p.n_planes && p.cand_count[threadIdx.x] > (unsigned)p.per_plane;
+    if (over[threadIdx.x]) atomicAdd(&n_over, 1);
+  }
+  __syncthreads();
+  if (n_over == 0) {
+    // every plane keeps all its hits: no histogram, no boundary bucket (the
+    // counts are final, so every CTA takes this branch)
+    if (blockIdx.x == 0 && threadIdx.x < p.n_planes) p.sel_bucket[threadIdx.x] = -1;
+    return;
+  }
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sh_hist[i] = 0u;
   __syncthreads();
   const unsigned n = min(*p.cand_total, (unsigned)p.cand_cap);
   // warp-uniform loop, kSelUnroll records per lane in flight; lanes that hit
