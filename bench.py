@@ -138,6 +138,22 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_peak():
+    """Dense BF16 tensor rate (TFLOP/s) for a kernel timed alone: the burst
+    figure of MEASURED_PEAKS.json, else the fallback measurement."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+# tensor-core work of one (tile, template) item in the precision form: the
+# inverse DFT as DFT-64 (M 128 x K 128 x N 32 per item) and DFT-32 (M 128 x
+# K 64 x N 64 per two items) real GEMMs, each as three split products
+# (hi*hi + hi*lo + lo*hi)
+TC_FLOPS_PER_ITEM = 3 * (2 * 128 * 128 * 32 + 2 * 64 * 64 * 64)
+
+
 # ------------------------------------------------------------------ CPU side
 def cpu_search(x, bank, thr, ex, workers):
     """One whole CPU search of the reference's path at its own precision:
@@ -667,6 +683,13 @@ def precision_form(bins=N_BINS, steps=50, warmup=3, noise_only=False):
             ref_keys = keys
         out[name] = {"searches_per_s": 1e3 / ms, "ms_per_search": ms, "ft_convolution_ms": float(st[2]),
                      "candidates": n_total, "same_candidates_as_fp32": keys == ref_keys}
+        if prec:  # tensor-core rate of the FT convolution stage against the dense BF16 peak
+            items = -(-args.bins // 1628) * N_TEMPLATES
+            flops = TC_FLOPS_PER_ITEM * items
+            peak, src = measured_bf16_peak()
+            achieved = flops / (float(st[2]) * 1e-3) / 1e12
+            out[name]["tensor"] = {"flops_per_search": flops, "achieved_tflops": achieved, "peak_tflops": peak,
+                                   "frac": achieved / peak, "peak_source": src}
         h.close()
     return {"form": "precision", "metric": "searches/s at 2^21 bins x 85 tmpl x 8 harm by DFT precision",
             "unit": "searches/s", "n_bins": args.bins, "steps": args.steps, "warmup": args.warmup,
