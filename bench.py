@@ -493,10 +493,17 @@ def served_form(rate, n_req, slots):
                 time.sleep(dt)
             t_sub.append(time.perf_counter())
             ids.append(srv.submit(pool[n][k], thr[P], rows_of(half)))
-        lat = [srv.result(rid)[3] for rid in ids]
-        # each request's result time = its submit time + the server-measured latency
-        wall = max(ts + l * 1e-3 for ts, l in zip(t_sub, lat)) - t0
+        lat_srv = [srv.result(rid)[3] for rid in ids]
+        # the server measures from the entry of submit (the spectrum's copy
+        # included); like the plain path below, each request's latency counts
+        # from its scheduled arrival, so a submitting loop that falls behind
+        # the arrivals is charged too
+        lag = [(ts - (t0 + ta)) * 1e3 for ts, ta in zip(t_sub, arrivals)]
+        lat = [g + l for g, l in zip(lag, lat_srv)]
+        wall = max(t0 + ta + l * 1e-3 for ta, l in zip(arrivals, lat)) - t0
         served = stats(lat, wall)
+        served["server_p50_ms"] = float(np.percentile(lat_srv, 50))
+        served["submit_lag_p99_ms"] = float(np.percentile(lag, 99))
         served["peak_in_flight"] = srv.stats()["peak_in_flight"]
 
     # ---- plain path per request: one handle per length class, searches one at a time

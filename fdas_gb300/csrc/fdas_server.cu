@@ -15,9 +15,17 @@
 // fdas_server_wait collects them.  Each request runs the same kernels on the
 // same inputs as a plain fdas_launch on its own handle, so its result does not
 // depend on what else is running.
+//
+// Latency: submit copies the spectrum straight into a pooled device buffer
+// (the driver reads pageable host memory far faster than a host copy into
+// pinned memory), the slot searches from there; a completer thread polls the
+// in-flight searches' events and collects results; the dispatcher, the
+// completer and fdas_server_wait spin (bounded, on the host) before they
+// block, since a wake-up costs tens of microseconds.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -40,12 +48,12 @@ double now_ms() {
 
 struct Request {
   uint64_t id = 0;
-  fdas_complex *spectrum = nullptr;  // pinned, from the server's pool (class_bins values)
+  fdas_complex *spectrum = nullptr;  // device memory, from the server's pool (class_bins values)
   uint32_t class_bins = 0;
   uint32_t n_bins = 0, row_begin = 0, n_templates = 0, n_planes = 0;
   std::vector<float> thresholds;
   double t_submit = 0, t_start = 0, t_done = 0;
-  bool done = false;
+  std::atomic<bool> done{false};
   fdas_status status = FDAS_OK;
   std::string error;
   std::vector<fdas_candidate> candidates;
@@ -57,9 +65,9 @@ struct Slot {
   uint32_t class_bins = 0;
   size_t bytes = 0;
   std::shared_ptr<Request> req;
-  uint32_t *loc = nullptr;          // pinned fixed-size list of the launch
-  float *pwr = nullptr;
   double t_idle = 0;
+  cudaEvent_t done = nullptr;  // recorded after the search's last step on the slot's stream
+  bool launched = false;       // a search is in flight (set and cleared under the server's lock)
 };
 
 }  // namespace
@@ -74,11 +82,13 @@ struct fdas_server {
   std::deque<std::shared_ptr<Request>> queue;
   std::map<uint64_t, std::shared_ptr<Request>> requests;
   uint64_t next_id = 1;
-  std::map<uint32_t, std::vector<fdas_complex *>> pinned;  // free request buffers per length class
-  std::deque<Slot *> finished;                            // searches whose stream has drained
+  std::map<uint32_t, std::vector<fdas_complex *>> pool;  // free device request buffers per length class
   std::mutex mu;
   std::condition_variable cv_work, cv_done, cv_finished;
-  bool stop = false;
+  // Bumped (under the lock) whenever the dispatcher may have work: a submit or
+  // a freed slot; and whenever the completer has a new search to watch.
+  std::atomic<uint64_t> work_seq{0}, launch_seq{0};
+  std::atomic<bool> stop{false};
   std::thread worker, completer;
   std::string err;
   // statistics
@@ -94,11 +104,10 @@ uint32_t class_of(uint32_t n, uint32_t min_class, uint32_t max_bins) {
   return std::min(c, max_bins);
 }
 
-// frees a slot's device and pinned memory; `s` given: also its byte count
+// frees a slot's device memory; `s` given: also its byte count
 void release_slot(fdas_server *s, Slot *sl) {
+  if (sl->done) cudaEventDestroy(sl->done);
   fdas_destroy(sl->h);
-  cudaFreeHost(sl->loc);
-  cudaFreeHost(sl->pwr);
   if (s) s->used -= sl->bytes;
 }
 
@@ -124,10 +133,8 @@ std::unique_ptr<Slot> make_slot(fdas_server *s, uint32_t cls, std::string &err) 
     fdas_destroy(sl->h);
     return nullptr;
   }
-  const size_t list = (size_t)s->cfg.max_planes * 2048;
-  if (cudaHostAlloc((void **)&sl->loc, sizeof(uint32_t) * list, cudaHostAllocDefault) != cudaSuccess ||
-      cudaHostAlloc((void **)&sl->pwr, sizeof(float) * list, cudaHostAllocDefault) != cudaSuccess) {
-    err = "pinned host allocation failed";
+  if (cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess) {
+    err = "event creation failed";
     fdas_destroy(sl->h);
     return nullptr;
   }
@@ -168,58 +175,84 @@ void finish(Slot *sl, Request *r) {
   r->t_done = now_ms();
 }
 
-struct Done {
-  fdas_server *s;
-  Slot *sl;
-};
-
-// stream callback after a slot's search: hand the slot to the completer
-// (no CUDA call allowed here)
-void CUDART_CB on_drained(void *arg) {
-  Done *d = static_cast<Done *>(arg);
-  {
-    std::lock_guard<std::mutex> lk(d->s->mu);
-    d->s->finished.push_back(d->sl);
-  }
-  d->s->cv_finished.notify_one();
-  delete d;
-}
-
 fdas_status start(fdas_server *s, Slot *sl, Request *r) {
   fdas_status st = fdas_reshape(sl->h, r->n_bins, r->row_begin, r->n_templates, 0, r->n_planes);
   if (st != FDAS_OK) return st;
   r->t_start = now_ms();
-  st = fdas_launch(sl->h, r->spectrum, r->thresholds.data(), sl->loc, sl->pwr, FDAS_ALL_ACCELERATIONS, FDAS_SET_A);
+  // the spectrum is already in device memory (copied there by submit)
+  st = fdas_enqueue_search_device(sl->h, r->spectrum, r->thresholds.data(), FDAS_ALL_ACCELERATIONS, FDAS_SET_A);
   if (st != FDAS_OK) return st;
   cudaStream_t stream = static_cast<cudaStream_t>(fdas_get_stream(sl->h, FDAS_SET_A));
-  if (cudaLaunchHostFunc(stream, on_drained, new Done{s, sl}) != cudaSuccess) return FDAS_ERR_CUDA;
+  if (cudaEventRecord(sl->done, stream) != cudaSuccess) return FDAS_ERR_CUDA;
   return FDAS_OK;
 }
 
 void complete(fdas_server *s, const std::shared_ptr<Request> &r) {
-  s->pinned[r->class_bins].push_back(r->spectrum);
+  s->pool[r->class_bins].push_back(r->spectrum);
   r->spectrum = nullptr;
-  r->done = true;
+  r->done.store(true);
   ++s->n_completed;
   s->cv_done.notify_all();
 }
 
-// Completer thread: collects drained slots' results, frees the slots.
+// Spin (bounded, on the host) for up to `us` microseconds until `ready()`;
+// a wake-up from a blocking wait costs tens of microseconds, a search of a
+// short spectrum about a hundred.
+template <typename F>
+bool spin_until(F ready, double us) {
+  const double t_end = now_ms() + us * 1e-3;
+  while (!ready()) {
+    if (now_ms() > t_end) return false;
+    std::this_thread::yield();
+  }
+  return true;
+}
+
+// Completer thread: watches the searches in flight by polling their `done`
+// events (a stream callback would add a driver-thread hop and a wake-up),
+// collects each finished search's results and frees its slot.
 void completer(fdas_server *s) {
   cudaSetDevice(s->cfg.device);
   std::unique_lock<std::mutex> lk(s->mu);
+  std::vector<Slot *> flying;
   while (true) {
-    s->cv_finished.wait(lk, [&] { return s->stop || !s->finished.empty(); });
-    if (s->finished.empty()) break;  // stop requested and nothing left
-    Slot *sl = s->finished.front();
-    s->finished.pop_front();
-    auto r = sl->req;
+    flying.clear();
+    for (auto &sl : s->slots)
+      if (sl->req && sl->launched) flying.push_back(sl.get());
+    if (flying.empty()) {
+      if (s->stop) break;
+      const uint64_t seq = s->launch_seq.load();
+      lk.unlock();
+      const bool more = spin_until([&] { return s->launch_seq.load() != seq; }, 200.0);
+      lk.lock();
+      if (!more) s->cv_finished.wait(lk, [&] { return s->stop || s->launch_seq.load() != seq; });
+      continue;
+    }
+    const uint64_t seq = s->launch_seq.load();
     lk.unlock();
-    finish(sl, r.get());
+    Slot *ready = nullptr;
+    // poll the flying searches until one is done or another is launched
+    while (!ready) {
+      for (Slot *sl : flying)
+        if (cudaEventQuery(sl->done) != cudaErrorNotReady) {
+          ready = sl;
+          break;
+        }
+      if (ready || s->launch_seq.load() != seq) break;
+      std::this_thread::yield();
+    }
+    if (!ready) {
+      lk.lock();
+      continue;
+    }
+    auto r = ready->req;
+    finish(ready, r.get());
     lk.lock();
-    sl->req.reset();
-    sl->t_idle = r->t_done;
+    ready->launched = false;
+    ready->req.reset();
+    ready->t_idle = r->t_done;
     complete(s, r);
+    ++s->work_seq;
     s->cv_work.notify_one();
   }
 }
@@ -274,6 +307,11 @@ bool admit_one(fdas_server *s, std::unique_lock<std::mutex> &lk) {
       s->used += fresh->bytes;
       s->slots.push_back(std::move(fresh));
     }
+    if (st == FDAS_OK) {
+      pick->launched = true;  // the completer watches it from now on
+      ++s->launch_seq;
+      s->cv_finished.notify_one();
+    }
     if (st != FDAS_OK) {
       if (pick) pick->req.reset();
       r->status = st;
@@ -298,8 +336,12 @@ void dispatcher(fdas_server *s) {
   cudaSetDevice(s->cfg.device);
   std::unique_lock<std::mutex> lk(s->mu);
   while (!s->stop) {
+    const uint64_t seq = s->work_seq.load();
     if (admit_one(s, lk)) continue;
-    s->cv_work.wait(lk);  // woken by a submit or a freed slot
+    lk.unlock();
+    const bool more = spin_until([&] { return s->work_seq.load() != seq || s->stop; }, 200.0);
+    lk.lock();
+    if (!more) s->cv_work.wait(lk, [&] { return s->work_seq.load() != seq || s->stop; });
   }
 }
 
@@ -360,32 +402,44 @@ fdas_status fdas_server_submit(fdas_server *s, const fdas_complex *spectrum, uin
     return FDAS_ERR_INVALID_ARG;
   if (n_planes == 0 || n_planes > s->cfg.max_planes) return FDAS_ERR_INVALID_ARG;
   auto r = std::make_shared<Request>();
+  r->t_submit = now_ms();  // the request's latency includes its copy into the server's buffer
   r->class_bins = class_of(n_bins, s->cfg.min_class_bins, s->cfg.max_bins);
   {
     std::lock_guard<std::mutex> lk(s->mu);
-    auto &freelist = s->pinned[r->class_bins];
+    auto &freelist = s->pool[r->class_bins];
     if (!freelist.empty()) {
       r->spectrum = freelist.back();
       freelist.pop_back();
     }
   }
-  if (!r->spectrum &&
-      cudaHostAlloc((void **)&r->spectrum, sizeof(fdas_complex) * r->class_bins, cudaHostAllocDefault) != cudaSuccess) {
+  cudaSetDevice(s->cfg.device);
+  if (!r->spectrum && cudaMalloc((void **)&r->spectrum, sizeof(fdas_complex) * r->class_bins) != cudaSuccess) {
     cudaGetLastError();
     return FDAS_ERR_OUT_OF_MEMORY;
   }
-  std::memcpy(r->spectrum, spectrum, sizeof(fdas_complex) * n_bins);
+  // straight from the caller's memory into device memory, on this thread's
+  // own stream, finished before submit returns (the caller may reuse its
+  // buffer at once); the driver reads pageable memory at ~160 GB/s here, a
+  // host copy into pinned memory would run at 15-30 GB/s
+  if (cudaMemcpyAsync(r->spectrum, spectrum, sizeof(fdas_complex) * n_bins, cudaMemcpyDefault,
+                      cudaStreamPerThread) != cudaSuccess ||
+      cudaStreamSynchronize(cudaStreamPerThread) != cudaSuccess) {
+    cudaGetLastError();
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->pool[r->class_bins].push_back(r->spectrum);
+    return FDAS_ERR_CUDA;
+  }
   r->n_bins = n_bins;
   r->row_begin = template_row_begin;
   r->n_templates = n_templates;
   r->n_planes = n_planes;
   r->thresholds.assign(thresholds, thresholds + n_planes);
-  r->t_submit = now_ms();
   {
     std::lock_guard<std::mutex> lk(s->mu);
     r->id = s->next_id++;
     s->requests[r->id] = r;
     s->queue.push_back(r);
+    ++s->work_seq;
   }
   s->cv_work.notify_one();
   *request_id = r->id;
@@ -399,7 +453,13 @@ fdas_status fdas_server_wait(fdas_server *s, uint64_t request_id, int32_t timeou
   auto it = s->requests.find(request_id);
   if (it == s->requests.end()) return FDAS_ERR_INVALID_ARG;
   auto r = it->second;
-  auto ready = [&] { return r->done; };
+  auto ready = [&] { return r->done.load(); };
+  const double spin_us = timeout_ms < 0 ? 200.0 : std::min(200.0, 1e3 * timeout_ms);
+  if (!ready() && spin_us > 0) {  // a short spin first: most searches end within it
+    lk.unlock();
+    spin_until(ready, spin_us);
+    lk.lock();
+  }
   if (timeout_ms < 0) s->cv_done.wait(lk, ready);
   else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return FDAS_ERR_TIMEOUT;
   if (!out && capacity == 0) {  // counts only: the request stays to be collected
@@ -449,15 +509,17 @@ void fdas_server_destroy(fdas_server *s) {
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
+    ++s->work_seq;
+    ++s->launch_seq;
   }
   s->cv_work.notify_all();
   s->cv_finished.notify_all();
   if (s->worker.joinable()) s->worker.join();
   if (s->completer.joinable()) s->completer.join();
   for (auto &sl : s->slots) release_slot(s, sl.get());
-  for (auto &r : s->queue) cudaFreeHost(r->spectrum);
-  for (auto &kv : s->pinned)
-    for (auto *p : kv.second) cudaFreeHost(p);
+  for (auto &r : s->queue) cudaFree(r->spectrum);
+  for (auto &kv : s->pool)
+    for (auto *p : kv.second) cudaFree(p);
   delete s;
 }
 

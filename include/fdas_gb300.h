@@ -429,9 +429,11 @@ void fdas_server_default_config(fdas_server_config *cfg);
  * FDAS_TEMPLATES_TIME_DOMAIN, 2048 spectrum values otherwise). */
 fdas_status fdas_server_create(const fdas_server_config *cfg, const fdas_complex *bank, fdas_template_layout layout,
                                uint32_t bank_rows, uint32_t bank_len, fdas_server **out);
-/* Queue one search: n_bins spectrum values (copied), the bank rows
- * [template_row_begin, template_row_begin + n_templates) (odd count), n_planes
- * thresholds.  Returns at once with the request's id. */
+/* Queue one search: n_bins spectrum values (host or device memory; copied
+ * into the server's device memory before the call returns, so the caller may
+ * reuse its buffer), the bank rows [template_row_begin, template_row_begin +
+ * n_templates) (odd count), n_planes thresholds.  Returns with the request's
+ * id; the search runs asynchronously. */
 fdas_status fdas_server_submit(fdas_server *s, const fdas_complex *spectrum, uint32_t n_bins,
                                uint32_t template_row_begin, uint32_t n_templates, uint32_t n_planes,
                                const float *thresholds, uint64_t *request_id);
