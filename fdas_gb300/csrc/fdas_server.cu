@@ -98,6 +98,8 @@ struct fdas_server {
 
 namespace {
 
+constexpr int kPoolPerSlot = 2;  // request buffers a new slot adds to its class's pool
+
 uint32_t class_of(uint32_t n, uint32_t min_class, uint32_t max_bins) {
   uint32_t c = min_class;
   while (c < n) c <<= 1;
@@ -137,6 +139,24 @@ std::unique_ptr<Slot> make_slot(fdas_server *s, uint32_t cls, std::string &err) 
     err = "event creation failed";
     fdas_destroy(sl->h);
     return nullptr;
+  }
+  // request buffers of this class for the pool, allocated here on the
+  // dispatcher thread: a device allocation inside submit can stall the caller
+  // (tens of milliseconds were seen right after large frees)
+  fdas_complex *bufs[kPoolPerSlot] = {};
+  for (auto &b : bufs)
+    if (cudaMalloc((void **)&b, sizeof(fdas_complex) * cls) != cudaSuccess) {
+      cudaGetLastError();
+      b = nullptr;
+    }
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto &pool = s->pool[cls];
+    for (auto *b : bufs) {
+      if (!b) continue;
+      if (pool.size() < 2 * (size_t)s->cfg.max_slots) pool.push_back(b);  // slots come and go: keep it bounded
+      else cudaFree(b);
+    }
   }
   size_t free1 = 0;
   cudaMemGetInfo(&free1, &total);
