@@ -2,7 +2,7 @@
 include/fdas_gb300.h).
 
     srv = Server(bank)                      # bank resident on the device
-    rid = srv.submit(spectrum, thresholds)  # returns at once
+    rid = srv.submit(spectrum, thresholds)  # copies the spectrum to the device, returns
     rec, n_total, n_dropped, latency_ms = srv.result(rid)
 
 Requests of any length up to ``max_bins``, with the full bank or a contiguous
