@@ -432,23 +432,30 @@ fdas_status fdas_server_submit(fdas_server *s, const fdas_complex *spectrum, uin
       freelist.pop_back();
     }
   }
+  int caller_dev = 0;  // the caller's current device is left as it was
+  cudaGetDevice(&caller_dev);
   cudaSetDevice(s->cfg.device);
+  fdas_status st = FDAS_OK;
   if (!r->spectrum && cudaMalloc((void **)&r->spectrum, sizeof(fdas_complex) * r->class_bins) != cudaSuccess) {
     cudaGetLastError();
-    return FDAS_ERR_OUT_OF_MEMORY;
+    r->spectrum = nullptr;
+    st = FDAS_ERR_OUT_OF_MEMORY;
   }
   // straight from the caller's memory into device memory, on this thread's
   // own stream, finished before submit returns (the caller may reuse its
   // buffer at once); the driver reads pageable memory at ~160 GB/s here, a
   // host copy into pinned memory would run at 15-30 GB/s
-  if (cudaMemcpyAsync(r->spectrum, spectrum, sizeof(fdas_complex) * n_bins, cudaMemcpyDefault,
-                      cudaStreamPerThread) != cudaSuccess ||
-      cudaStreamSynchronize(cudaStreamPerThread) != cudaSuccess) {
+  if (st == FDAS_OK &&
+      (cudaMemcpyAsync(r->spectrum, spectrum, sizeof(fdas_complex) * n_bins, cudaMemcpyDefault,
+                       cudaStreamPerThread) != cudaSuccess ||
+       cudaStreamSynchronize(cudaStreamPerThread) != cudaSuccess)) {
     cudaGetLastError();
     std::lock_guard<std::mutex> lk(s->mu);
     s->pool[r->class_bins].push_back(r->spectrum);
-    return FDAS_ERR_CUDA;
+    st = FDAS_ERR_CUDA;
   }
+  cudaSetDevice(caller_dev);
+  if (st != FDAS_OK) return st;
   r->n_bins = n_bins;
   r->row_begin = template_row_begin;
   r->n_templates = n_templates;
