@@ -47,6 +47,7 @@ class FdasConfig(ctypes.Structure):
         ("trace_enqueue", ctypes.c_uint32),
         ("log_fn", LOG_FN),
         ("log_user", ctypes.c_void_p),
+        ("stream_priority", ctypes.c_int32),
     ]
 
 

@@ -686,7 +686,7 @@ fdas_status fdas_initialise_accelerator(const fdas_config *cfg_in, fdas_handle *
         (e = cudaMemset(S.d_ctrl, 0, sizeof(unsigned) * kCtrlStride)) != cudaSuccess ||
         (e = cudaHostAlloc((void **)&S.h_ctrl, sizeof(unsigned) * kCtrlStride, cudaHostAllocDefault)) !=
             cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        (e = cudaStreamCreateWithPriority(&S.stream, cudaStreamNonBlocking, h->cfg.stream_priority)) != cudaSuccess) {
       cuda_fail(h, e, "buffer set initialisation", __FILE__, __LINE__);
       return bail(FDAS_ERR_CUDA);
     }

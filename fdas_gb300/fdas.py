@@ -90,11 +90,12 @@ class FDAS:
     def initialise_accelerator(self, input_sz, mode=PerSet, sync_pipeline=False, device=0, n_templates=85,
                                max_template_len=421, tile_overlap=0, n_planes=8, candidate_capacity=0,
                                candidates_per_plane_compat=0, recheck=True, recheck_band=0.0, overlap=False,
-                               precision=0, trace_enqueue=False):
+                               precision=0, trace_enqueue=False, stream_priority=0):
         """FDAS::initialise_accelerator (FDAS.h:44-49).  The bitstream and the
         OpenCL platform / device selectors become a CUDA device ordinal.
         ``trace_enqueue``: log the reference's per-launch "[INFO] Enqueueing" and
-        "%%%" lines (FDAS.cpp:556-575)."""
+        "%%%" lines (FDAS.cpp:556-575).  ``stream_priority``: CUDA priority of
+        the buffer sets' streams (0 default, negative higher)."""
         cfg = _lib.FdasConfig()
         self._lib.fdas_default_config(ctypes.byref(cfg), int(input_sz))
         cfg.n_templates = n_templates
@@ -111,6 +112,7 @@ class FDAS:
         cfg.overlap = int(bool(overlap))
         cfg.precision = int(precision)
         cfg.trace_enqueue = int(bool(trace_enqueue))
+        cfg.stream_priority = int(stream_priority)
         cfg.log_fn = self._log_cb  # the "^^^" line of initialisation goes to this log too
         cfg.log_user = None
         if self._h:

@@ -119,6 +119,9 @@ typedef struct {
                                   of fdas_initialise_accelerator go here, like every later
                                   line of the handle (fdas_set_log changes it) */
   void *log_user;              /* passed to log_fn */
+  int32_t stream_priority;     /* CUDA priority of the buffer sets' streams: 0 (default) the
+                                  default priority, negative values higher ones (the range is
+                                  cudaDeviceGetStreamPriorityRange's; CUDA clamps others) */
 } fdas_config;
 
 /* Fill `cfg` with the reference's defaults for `n_frequency_bins` bins. */

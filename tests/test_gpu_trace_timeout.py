@@ -190,3 +190,21 @@ def test_server_wait_expires_then_collects():
     assert ok, p.last_error
     want, want_total, _ = p.retrieve_candidate_list(FDAS.A)
     assert total == want_total and np.array_equal(rec, want)
+
+
+def test_stream_priority_same_results():
+    """fdas_config.stream_priority only orders work on the device: a handle
+    on high-priority streams gives the same candidate lists."""
+    x, thr = _case(n=1 << 15, seed=7)
+    bank = template_bank()
+    out = []
+    for prio in (0, -5):
+        p = make_pipeline(x.size, log=io.StringIO(), stream_priority=prio)
+        assert p.upload_templates(bank, FDAS.A)
+        ok, loc, pwr = _search(p, x, thr)
+        assert ok, p.last_error
+        rec, _, _ = p.retrieve_candidate_list(FDAS.A)
+        out.append((loc, pwr, rec))
+        p.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
